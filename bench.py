@@ -1,0 +1,340 @@
+"""Benchmark: traced source rays per second on the triangle-mesh cylindrical hole.
+
+Workload (one "step" = one trace of the whole ray batch): cylindrical hole of
+radius 0.5 and depth 10 in a 2 x 2 x/y-periodic cell, 200,192 float32
+triangles from a seeded structured tessellation with +-1 % vertex jitter,
+cosine source (exponent 1) on the plane z = 0.1, sticking 0.01, 10 % specular /
+90 % diffuse re-emission, 1e7 source rays per step.  Inputs are synthetic.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours: librtg on the GPU.  `value` = rays / device time of the traces with the
+geometry resident in HBM (L2 flushed between steps by a 256 MB write);
+`e2e` = the same metric through the public API from host arrays (geometry
+upload + LBVH build + trace + reading counts and S1 back) per step.
+reference: the CPU restatement of rti's tracer (oracle/) on all host cores,
+each step a bounded sample of the same workload.
+Under torchrun each rank traces its own ray range (weak scaling) and the
+per-primitive accumulators are summed across ranks with NCCL.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "traced rays/s"
+UNIT = "rays/s"
+N_RAYS = 10_000_000
+STICKING = 0.01
+SPECULAR = 0.1
+
+
+def workload():
+    from rti_gb300 import scenes
+    return scenes.hole_triangles(radius=0.5, depth=10.0, cell=2.0, n_theta=512, n_wall=160, n_top=24, n_bottom=12,
+                                 jitter=0.01, seed=0, source_gap=0.1)
+
+
+def config_dict(h, n_rays):
+    return {"workload": "hole_triangles", "radius": 0.5, "depth": 10.0, "cell": "2x2 periodic",
+            "n_triangles": int(h.n), "n_rays_per_step": int(n_rays), "sticking": STICKING,
+            "specular_fraction": SPECULAR, "source_exponent": 1.0, "source_plane_z": 0.1,
+            "l2": "flushed between steps (256 MB write)", "parallelism": "rays sharded per rank (weak scaling)"}
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_traffic():
+    """Per-launch DRAM bytes of the path kernel from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "trace_paths_hole.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = max(mx, float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(h, n_rays, nthreads, seed=0):
+    """Times the oracle on `n_rays` rays of the workload; returns rays/s."""
+    from oracle import oracle as O
+    s = O.Scene(tri_vertices=h.vertices, tri_indices=h.indices)
+    cfg = O.make_config(h.box_lo, h.box_hi, sticking=STICKING, reflection=2, specular_fraction=SPECULAR, seed=seed)
+    t0 = time.perf_counter()
+    r = s.trace(cfg, 0, n_rays, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return n_rays / dt, r
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    h = workload()
+    cores = os.cpu_count() or 1
+    sample = args.ref_rays
+    s = O.Scene(tri_vertices=h.vertices, tri_indices=h.indices)
+    cfg = O.make_config(h.box_lo, h.box_hi, sticking=STICKING, reflection=2, specular_fraction=SPECULAR)
+    for w in range(args.warmup):
+        cfg.seed = 1000 + w
+        s.trace(cfg, 0, sample, nthreads=cores)
+    times = []
+    for k in range(args.steps):
+        cfg.seed = k
+        t0 = time.perf_counter()
+        s.trace(cfg, 0, sample, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = sample * args.steps / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f64 accumulators", "data": "synthetic",
+            "impl": "reference", "config": config_dict(h, sample),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{sample} source rays of the workload per step, all host threads; "
+                                       "C restatement of rti's tracer (rti's Embree path does not build here)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+class _CAI:
+    """__cuda_array_interface__ view of a device buffer (for torch.as_tensor)."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from rti_gb300 import Engine
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    h = workload()
+    R = args.rays
+    eng = Engine(local)
+    eng.upload_triangles(h.vertices, h.indices)
+    eng.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
+                  x_bound=1, y_bound=1, source_exponent=1.0)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    view = eng.device_view()
+    acc = None
+    if world > 1:
+        acc = torch.as_tensor(_CAI(view.s1, 4 * view.n, "<f8"), device=dev)
+        cnt = torch.as_tensor(_CAI(view.counts, view.n, "<i8"), device=dev)
+
+    def step(k):
+        eng.trace(R, seed=k, stream=stream.cuda_stream, ray_begin=rank * R)
+        if world > 1:
+            dist.all_reduce(acc)
+            dist.all_reduce(cnt)
+
+    for w in range(args.warmup):
+        flush.zero_()
+        step(10_000 + w)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    kernel_ms, segs, tallies = [], 0, []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            step(k)
+            ev[k][1].record(stream)
+            t = eng.tally()  # synchronises; read outside the event pair
+            kernel_ms.append(t.kernel_ms)
+            tallies.append(t)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        wall = time.perf_counter() - t0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([dev_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_s = float(tt.item())
+    value = world * R * args.steps / dev_s
+    clocks = clk.summary()
+
+    # roofline of the path kernel: algorithmic bytes per launch / its event time
+    seg = statistics.mean(t.segments for t in tallies)
+    dep = statistics.mean(t.hitc + t.nb_deposits for t in tallies)
+    levels = math.ceil(math.log2(max(h.n / 4, 2)))
+    prim_bytes = 48
+    alg_bytes = seg * (64 + 64 * levels + 4 * prim_bytes) + 16 * dep
+    kms = statistics.mean(kernel_ms)
+    achieved = alg_bytes / (kms / 1e3) / 1e9
+    peak, peak_kind = read_peaks()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": read_traffic(), "peak_source": peak_kind, "kernel": "trace_paths_kernel",
+            "kernel_ms": kms, "segments_per_launch": seg, "alg_bytes_per_launch": alg_bytes,
+            "bytes_per_segment_model": f"64 + 64*{levels} + 4*{prim_bytes} (+16 per deposit)"}
+
+    # end to end through the public API from host arrays
+    e2e = None
+    if not args.no_e2e:
+        pin_v = torch.from_numpy(h.vertices).pin_memory().numpy()
+        pin_i = torch.from_numpy(h.indices.view(np.int32)).pin_memory().numpy().view(np.uint32)
+        e2e_times = []
+        for k in range(args.e2e_steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2 = Engine(local)
+            e2.upload_triangles(pin_v, pin_i)
+            e2.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
+                         x_bound=1, y_bound=1)
+            e2.trace(R, seed=k, ray_begin=rank * R)
+            c = e2.hit_counts()
+            s1 = e2.values()
+            e2.close()
+            dt = time.perf_counter() - t0
+            if k > 0:
+                e2e_times.append(dt)
+        del c, s1
+        np_ = h.n
+        e2e = {"value": world * R / statistics.mean(e2e_times), "unit": UNIT,
+               "h2d_bytes_per_step": int(16 * len(h.vertices) + 12 * h.n),
+               "d2h_bytes_per_step": int(16 * np_),
+               "includes": "context creation, upload, LBVH build, trace, hit counts + S1 read back"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rays_s, _ = cpu_sample(h, args.cpu_rays, os.cpu_count() or 1)
+        cpu = {"value": rays_s, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{args.cpu_rays} source rays of the same workload, all host threads"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f64 accumulators",
+                "data": "synthetic", "config": config_dict(h, R), "clocks": clocks, "roofline": roof,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps,
+                "wall_s_timed_region": wall,
+                "tally_per_step": {"segments": seg, "hitc": statistics.mean(t.hitc for t in tallies),
+                                   "truncated": max(t.truncated for t in tallies),
+                                   "errors": max(t.errors for t in tallies)}}
+        print(json.dumps(line))
+    eng.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--rays", type=int, default=N_RAYS)
+    ap.add_argument("--cpu-rays", type=int, default=2_000_000, help="CPU-baseline sample (ours arm)")
+    ap.add_argument("--ref-rays", type=int, default=500_000, help="rays per step of the reference arm")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    from __graft_entry__ import build
+    if args.impl == "reference":
+        from oracle import oracle
+        oracle.build()
+        run_reference(args)
+    else:
+        build()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+/*
+ * rtg.h -- C ABI of the GB300 flux engine (librtg.so).
+ *
+ * The engine computes Monte Carlo particle flux onto surfaces made of
+ * oriented discs and/or triangles, the job of rti::device / rti::trace::tracer
+ * in the rti library.  Every entry point takes plain pointers and sizes, returns
+ * an int status (RTG_OK = 0) and never throws; rtg_last_error() describes the
+ * last failure on a context.  One context belongs to one host thread at a
+ * time.  Host arrays are read during the call and not retained.
+ *
+ * Reference interfaces replaced (paths within the rti project):
+ *   rtg_create / rtg_destroy        device.hpp:42-45 (ctor), :84-85,:101 (Embree device)
+ *   rtg_upload_discs                device.hpp:47-60 set_points/set_normals/set_grid_spacing,
+ *                                   device.hpp:86-88, point_cloud_disc_geometry.hpp:119-232
+ *   rtg_upload_triangles            triangle_geometry.hpp:56-99, i_triangle_reader.hpp:22-38
+ *   rtg_upload_mixed                (no counterpart: discs and triangles in one scene)
+ *   rtg_update_discs / _vertices    (no counterpart: bounding-box refit for moved surfaces)
+ *   rtg_config_default/rtg_set_config  device.hpp:62-80 set_number_of_rays/set_x/set_y/set,
+ *                                   tracer.hpp:179 (tnear), rejection_control.hpp:16,22
+ *   rtg_set_sticking / _field       i_particle.hpp:14 get_sticking_probability
+ *   rtg_trace                       tracer.hpp:66-330 tracer::run
+ *   rtg_trace_rays                  tracer.hpp:181 rtcIntersect1 on caller-given rays
+ *   rtg_get_mc_estimates            device.hpp:109-112, :154-187
+ *   rtg_get_hit_counts              device.hpp:114-117, hit_accumulator.hpp:144-146
+ *   rtg_get_accumulators            hit_accumulator.hpp:140-142 (values, S1..S4)
+ *   rtg_get_exposed_areas           hit_accumulator.hpp:256-259, tracer.hpp:385-413
+ *   rtg_get_relative_error/_vov     hit_accumulator.hpp:152-249
+ *   rtg_get_tally                   result.hpp:11-33 (numRays, hitc, nonhitc, time)
+ *   rtg_get_neighbors               point_cloud_disc_geometry.hpp:103-106
+ *   rtg_device_run                  device.hpp:82-107 device::run in one call
+ */
+#ifndef RTG_H
+#define RTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTG_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define RTG_API __attribute__((visibility("default")))
+#else
+#define RTG_API
+#endif
+
+/* status codes */
+#define RTG_OK 0
+#define RTG_ERR_INVALID_ARGUMENT 1
+#define RTG_ERR_CUDA 2
+#define RTG_ERR_OUT_OF_MEMORY 3
+#define RTG_ERR_NO_GEOMETRY 4
+#define RTG_ERR_BUDGET 5      /* a device-side iteration limit was reached */
+#define RTG_ERR_ABORTED 6     /* rtg_request_abort() stopped a trace */
+#define RTG_ERR_INTERNAL 7
+
+/* boundary conditions: rti::geo::bound_condition (bound_condition.hpp:4-6) */
+#define RTG_BOUND_REFLECTIVE 0
+#define RTG_BOUND_PERIODIC 1
+
+/* re-emission: diffuse.hpp, specular.hpp, or a mixture of both */
+#define RTG_REFLECT_DIFFUSE 0
+#define RTG_REFLECT_SPECULAR 1
+#define RTG_REFLECT_MIXED 2
+
+/* box_mode */
+#define RTG_BOX_FROM_GEOMETRY 0 /* rti rule: x/y = centre extents, top = max z + 2 r_max */
+#define RTG_BOX_EXPLICIT 1      /* box_lo/box_hi as given (box_hi[2] is the source plane) */
+
+typedef struct rtg_context rtg_context;
+
+typedef struct rtg_config {
+  int32_t  x_bound;            /* RTG_BOUND_*; rti default REFLECTIVE (device.hpp:292) */
+  int32_t  y_bound;
+  int32_t  reflection;         /* RTG_REFLECT_* */
+  float    specular_fraction;  /* probability of a specular bounce for RTG_REFLECT_MIXED */
+  float    sticking;           /* global sticking probability (used when no field is set) */
+  float    source_exponent;    /* cos^n source; 1 = rti's cosine_direction_z */
+  int32_t  box_mode;           /* RTG_BOX_* */
+  float    box_lo[3];
+  float    box_hi[3];
+  float    tnear;              /* 1e-4 (tracer.hpp:179, source.hpp:32) */
+  double   roulette_threshold; /* 0.1 (rejection_control.hpp:16) */
+  double   roulette_weight;    /* 0.3 (rejection_control.hpp:22) */
+  uint32_t max_segments;       /* closest-hit queries per path before it is cut */
+  uint32_t job;                /* random-stream tag; 0 for a plain trace */
+} rtg_config;
+
+typedef struct rtg_tally {
+  uint64_t num_rays;     /* result.hpp numRays */
+  uint64_t hitc;         /* front-face hits (tracer.hpp:229) */
+  uint64_t nonhitc;      /* paths that left through the top/bottom (tracer.hpp:186) */
+  uint64_t total;        /* accumulator uses (hit_accumulator mTotalCnts) */
+  uint64_t segments;     /* closest-hit queries */
+  uint64_t truncated;    /* paths cut at max_segments */
+  uint64_t nb_deposits;  /* neighbour deposits (tracer.hpp:371) */
+  uint64_t errors;       /* device-side guard trips (stack/iteration limits) */
+  double   trace_ms;     /* device time of the last rtg_trace (zeroing + paths + areas) */
+  double   kernel_ms;    /* device time of the path kernel alone in the last rtg_trace */
+} rtg_tally;
+
+/* Fills *cfg with rti's defaults. */
+RTG_API void rtg_config_default(rtg_config* cfg);
+RTG_API int  rtg_abi_version(void);
+
+RTG_API int  rtg_create(rtg_context** ctx, int device);
+RTG_API int  rtg_destroy(rtg_context* ctx);
+RTG_API const char* rtg_last_error(const rtg_context* ctx);
+
+/* points: n x 3 centres, normals: n x 3 unit normals, radii: n (rti's "grid
+ * spacing", used as the disc radius, device.hpp:213-216).  Builds the LBVH and
+ * the neighbour lists.  Replaces any previous geometry; clears the sticking
+ * field. */
+RTG_API int rtg_upload_discs(rtg_context* ctx, const float* points, const float* normals, const float* radii,
+                     int64_t n);
+/* vertices: nv x 3, indices: nt x 3 (uint32).  Replaces any previous geometry. */
+RTG_API int rtg_upload_triangles(rtg_context* ctx, const float* vertices, const uint32_t* indices, int64_t nv,
+                         int64_t nt);
+/* Discs and triangles in one surface: primitive ids are the discs 0..nd-1,
+ * then the triangles nd..nd+nt-1.  Either part may be empty. */
+RTG_API int rtg_upload_mixed(rtg_context* ctx, const float* points, const float* normals, const float* radii, int64_t nd,
+                     const float* vertices, const uint32_t* indices, int64_t nv, int64_t nt);
+/* Moves the surface without changing its topology: refits the LBVH boxes and
+ * rebuilds the neighbour lists; the tree itself is kept. */
+RTG_API int rtg_update_discs(rtg_context* ctx, const float* points, const float* normals, const float* radii,
+                     int64_t n);
+RTG_API int rtg_update_vertices(rtg_context* ctx, const float* vertices, int64_t nv);
+
+RTG_API int rtg_set_config(rtg_context* ctx, const rtg_config* cfg);
+RTG_API int rtg_get_config(const rtg_context* ctx, rtg_config* cfg);
+/* The box the trace uses (after RTG_BOX_FROM_GEOMETRY is resolved). */
+RTG_API int rtg_get_box(const rtg_context* ctx, float* box_lo3, float* box_hi3);
+RTG_API int rtg_set_sticking(rtg_context* ctx, float sticking);
+/* per-primitive sticking (length = number of primitives); NULL clears it */
+RTG_API int rtg_set_sticking_field(rtg_context* ctx, const float* sticking, int64_t n);
+
+/* Traces source rays [0, n_rays) with Philox seed `seed` on `stream`
+ * (a cudaStream_t, NULL = the context's stream).  Zeroes the accumulators,
+ * traces, computes the exposed areas; returns after enqueueing.  The results
+ * are read with the getters below (which synchronise). */
+RTG_API int rtg_trace(rtg_context* ctx, uint64_t n_rays, uint64_t seed, void* stream);
+/* Same, for the ray range [ray_begin, ray_end) and accumulating into the
+ * current totals when accumulate != 0 (used to shard rays across GPUs). */
+RTG_API int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t seed,
+                    int accumulate, void* stream);
+RTG_API int rtg_synchronize(rtg_context* ctx);
+/* Asks a running trace to stop; it returns RTG_ERR_ABORTED. */
+RTG_API int rtg_request_abort(rtg_context* ctx);
+
+/* Closest hit for explicit rays: rays = n x 6 floats (origin, direction),
+ * host pointers.  prim_out = primitive id or -1, t_out = distance. */
+RTG_API int rtg_trace_rays(rtg_context* ctx, const float* rays, int64_t n, float tnear, int32_t* prim_out,
+                   float* t_out);
+
+/* Results (host buffers of the number of primitives). */
+RTG_API int rtg_num_primitives(const rtg_context* ctx, int64_t* n);
+RTG_API int rtg_get_mc_estimates(rtg_context* ctx, float* out);
+RTG_API int rtg_get_hit_counts(rtg_context* ctx, uint64_t* out);
+RTG_API int rtg_get_accumulators(rtg_context* ctx, double* s1, double* s2, double* s3, double* s4);
+RTG_API int rtg_get_exposed_areas(rtg_context* ctx, float* out);
+RTG_API int rtg_get_relative_error(rtg_context* ctx, double* out);
+RTG_API int rtg_get_vov(rtg_context* ctx, double* out);
+RTG_API int rtg_get_tally(rtg_context* ctx, rtg_tally* out);
+/* Neighbour CSR of the discs: row_ptr (nd+1), cols (cap entries); *nnz gets the count. */
+RTG_API int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols, int64_t cap, int64_t* nnz);
+
+/* Device-resident views (valid until the geometry changes). */
+typedef struct rtg_device_view {
+  double*   s1;        /* S1..S4 are consecutive arrays of n doubles */
+  double*   s2;
+  double*   s3;
+  double*   s4;
+  uint64_t* counts;
+  float*    areas;
+  float*    estimates;
+  int64_t   n;
+} rtg_device_view;
+RTG_API int rtg_get_device_view(rtg_context* ctx, rtg_device_view* view);
+
+/* device::run in one call (device.hpp:82-107): host arrays in, normalised
+ * smoothed estimates and hit counts out.  sticking_field may be NULL. */
+RTG_API int rtg_device_run(const float* points, const float* normals, const float* radii, int64_t n,
+                   const rtg_config* cfg, const float* sticking_field, uint64_t n_rays, uint64_t seed,
+                   float* mc_estimates_out, uint64_t* hit_counts_out, int device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

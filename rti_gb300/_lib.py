@@ -1,0 +1,144 @@
+"""ctypes bindings of librtg.so (the C ABI in include/rtg.h).
+
+The library is loaded from this package directory only; there is no fallback.
+If it is missing, build it with ``python -m rti_gb300.build`` (nvcc, sm_103a).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librtg.so")
+
+RTG_OK = 0
+RTG_ERR_INVALID_ARGUMENT = 1
+RTG_ERR_CUDA = 2
+RTG_ERR_OUT_OF_MEMORY = 3
+RTG_ERR_NO_GEOMETRY = 4
+RTG_ERR_BUDGET = 5
+RTG_ERR_ABORTED = 6
+RTG_ERR_INTERNAL = 7
+
+RTG_BOUND_REFLECTIVE = 0
+RTG_BOUND_PERIODIC = 1
+RTG_REFLECT_DIFFUSE = 0
+RTG_REFLECT_SPECULAR = 1
+RTG_REFLECT_MIXED = 2
+RTG_BOX_FROM_GEOMETRY = 0
+RTG_BOX_EXPLICIT = 1
+
+# every function include/rtg.h declares (checked by the tests)
+EXPORTS = [
+    "rtg_config_default", "rtg_abi_version", "rtg_create", "rtg_destroy", "rtg_last_error",
+    "rtg_upload_discs", "rtg_upload_triangles", "rtg_upload_mixed", "rtg_update_discs", "rtg_update_vertices",
+    "rtg_set_config", "rtg_get_config", "rtg_get_box", "rtg_set_sticking", "rtg_set_sticking_field",
+    "rtg_trace", "rtg_trace_range", "rtg_synchronize", "rtg_request_abort", "rtg_trace_rays",
+    "rtg_num_primitives", "rtg_get_mc_estimates", "rtg_get_hit_counts", "rtg_get_accumulators",
+    "rtg_get_exposed_areas", "rtg_get_relative_error", "rtg_get_vov", "rtg_get_tally",
+    "rtg_get_neighbors", "rtg_get_device_view", "rtg_device_run",
+]
+
+
+class RtgConfig(C.Structure):
+    _fields_ = [
+        ("x_bound", C.c_int32),
+        ("y_bound", C.c_int32),
+        ("reflection", C.c_int32),
+        ("specular_fraction", C.c_float),
+        ("sticking", C.c_float),
+        ("source_exponent", C.c_float),
+        ("box_mode", C.c_int32),
+        ("box_lo", C.c_float * 3),
+        ("box_hi", C.c_float * 3),
+        ("tnear", C.c_float),
+        ("roulette_threshold", C.c_double),
+        ("roulette_weight", C.c_double),
+        ("max_segments", C.c_uint32),
+        ("job", C.c_uint32),
+    ]
+
+
+class RtgTally(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in
+                ("num_rays", "hitc", "nonhitc", "total", "segments", "truncated", "nb_deposits", "errors")] + [
+        ("trace_ms", C.c_double), ("kernel_ms", C.c_double)]
+
+
+class RtgDeviceView(C.Structure):
+    _fields_ = [("s1", C.c_void_p), ("s2", C.c_void_p), ("s3", C.c_void_p), ("s4", C.c_void_p),
+                ("counts", C.c_void_p), ("areas", C.c_void_p), ("estimates", C.c_void_p), ("n", C.c_int64)]
+
+
+class RtgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"rtg error {code}: {msg}")
+        self.code = code
+
+
+_f32p = C.POINTER(C.c_float)
+_f64p = C.POINTER(C.c_double)
+_u64p = C.POINTER(C.c_uint64)
+_i64p = C.POINTER(C.c_int64)
+_i32p = C.POINTER(C.c_int32)
+_u32p = C.POINTER(C.c_uint32)
+_ctx = C.c_void_p
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads librtg.so; raises if it has not been built (there is no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"librtg.so not found at {p}; build it with `python -m rti_gb300.build`")
+    L = C.CDLL(p)
+    sig = {
+        "rtg_config_default": (None, [C.POINTER(RtgConfig)]),
+        "rtg_abi_version": (C.c_int, []),
+        "rtg_create": (C.c_int, [C.POINTER(_ctx), C.c_int]),
+        "rtg_destroy": (C.c_int, [_ctx]),
+        "rtg_last_error": (C.c_char_p, [_ctx]),
+        "rtg_upload_discs": (C.c_int, [_ctx, _f32p, _f32p, _f32p, C.c_int64]),
+        "rtg_upload_triangles": (C.c_int, [_ctx, _f32p, _u32p, C.c_int64, C.c_int64]),
+        "rtg_upload_mixed": (C.c_int, [_ctx, _f32p, _f32p, _f32p, C.c_int64, _f32p, _u32p, C.c_int64, C.c_int64]),
+        "rtg_update_discs": (C.c_int, [_ctx, _f32p, _f32p, _f32p, C.c_int64]),
+        "rtg_update_vertices": (C.c_int, [_ctx, _f32p, C.c_int64]),
+        "rtg_set_config": (C.c_int, [_ctx, C.POINTER(RtgConfig)]),
+        "rtg_get_config": (C.c_int, [_ctx, C.POINTER(RtgConfig)]),
+        "rtg_get_box": (C.c_int, [_ctx, _f32p, _f32p]),
+        "rtg_set_sticking": (C.c_int, [_ctx, C.c_float]),
+        "rtg_set_sticking_field": (C.c_int, [_ctx, _f32p, C.c_int64]),
+        "rtg_trace": (C.c_int, [_ctx, C.c_uint64, C.c_uint64, C.c_void_p]),
+        "rtg_trace_range": (C.c_int, [_ctx, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]),
+        "rtg_synchronize": (C.c_int, [_ctx]),
+        "rtg_request_abort": (C.c_int, [_ctx]),
+        "rtg_trace_rays": (C.c_int, [_ctx, _f32p, C.c_int64, C.c_float, _i32p, _f32p]),
+        "rtg_num_primitives": (C.c_int, [_ctx, _i64p]),
+        "rtg_get_mc_estimates": (C.c_int, [_ctx, _f32p]),
+        "rtg_get_hit_counts": (C.c_int, [_ctx, _u64p]),
+        "rtg_get_accumulators": (C.c_int, [_ctx, _f64p, _f64p, _f64p, _f64p]),
+        "rtg_get_exposed_areas": (C.c_int, [_ctx, _f32p]),
+        "rtg_get_relative_error": (C.c_int, [_ctx, _f64p]),
+        "rtg_get_vov": (C.c_int, [_ctx, _f64p]),
+        "rtg_get_tally": (C.c_int, [_ctx, C.POINTER(RtgTally)]),
+        "rtg_get_neighbors": (C.c_int, [_ctx, _i64p, _i32p, C.c_int64, _i64p]),
+        "rtg_get_device_view": (C.c_int, [_ctx, C.POINTER(RtgDeviceView)]),
+        "rtg_device_run": (C.c_int, [_f32p, _f32p, _f32p, C.c_int64, C.POINTER(RtgConfig), _f32p, C.c_uint64,
+                                     C.c_uint64, _f32p, _u64p, C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def default_config() -> RtgConfig:
+    c = RtgConfig()
+    load().rtg_config_default(C.byref(c))
+    return c

@@ -1,0 +1,660 @@
+// rtg_api.cu -- the C ABI of librtg (declared in include/rtg.h).
+//
+// A context owns one GPU's copy of a surface: primitive data by id and in
+// LBVH slot order, the LBVH, the neighbour lists, the sticking field and the
+// per-primitive accumulators.  rtg_trace enqueues the zeroing of the
+// accumulators, the persistent path kernel and the exposed-area kernel on one
+// stream, the span that rti times in tracer::run (tracer.hpp:122-286).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rtg_internal.cuh"
+
+namespace rtg {
+
+int set_error(rtg_context* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int check_cuda(rtg_context* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return RTG_OK;
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();
+  return set_error(ctx, e == cudaErrorMemoryAllocation ? RTG_ERR_OUT_OF_MEMORY : RTG_ERR_CUDA, m);
+}
+
+namespace {
+
+int use_device(rtg_context* ctx) {
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  return RTG_OK;
+}
+
+bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+int alloc_results(rtg_context* ctx) {
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  const size_t n = (size_t)(np > 0 ? np : 1);
+  RTG_TRY(dalloc(ctx, ctx->acc, 4 * n, "accumulators"));
+  RTG_TRY(dalloc(ctx, ctx->cnt, n, "hit counts"));
+  RTG_TRY(dalloc(ctx, ctx->areas, n, "exposed areas"));
+  RTG_TRY(dalloc(ctx, ctx->est, n, "estimates"));
+  RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * n * sizeof(double), ctx->stream));
+  RTG_CUDA(ctx, cudaMemsetAsync(ctx->cnt.p, 0, n * sizeof(unsigned long long), ctx->stream));
+  ctx->traced = false;
+  ctx->finalized = false;
+  return RTG_OK;
+}
+
+// The trace box: explicit, or rti's rule (device.hpp:86-92, 225-237,
+// point_cloud_disc_geometry.hpp:83-87): x/y = centre extents, z from the
+// lowest centre to the highest centre + 2 r_max (source plane).
+void resolve_box(rtg_context* ctx) {
+  const rtg_config& c = ctx->cfg;
+  const Geometry& g = ctx->g;
+  if (c.box_mode == RTG_BOX_EXPLICIT) {
+    for (int a = 0; a < 3; ++a) {
+      ctx->box_lo[a] = c.box_lo[a];
+      ctx->box_hi[a] = c.box_hi[a];
+    }
+    return;
+  }
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  if (g.nd > 0)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = g.cmin[a];
+      hi[a] = g.cmax[a];
+    }
+  if (g.nt > 0)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], g.tri_min[a]);
+      hi[a] = std::max(hi[a], g.tri_max[a]);
+    }
+  float top = hi[2];
+  if (g.nd > 0) top = (hi[2] + g.rmax) + g.rmax;
+  for (int a = 0; a < 3; ++a) {
+    ctx->box_lo[a] = lo[a];
+    ctx->box_hi[a] = hi[a];
+  }
+  ctx->box_hi[2] = top;
+}
+
+int upload_discs_impl(rtg_context* ctx, const float* pts, const float* nrm, const float* rad, int64_t n,
+                      bool rebuild) {
+  if (n < 0 || (n > 0 && (!pts || !nrm || !rad)))
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "discs: null array or negative count");
+  std::vector<float4> cr((size_t)n), nn((size_t)n);
+  Geometry& g = ctx->g;
+  float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  float rmax = 0.0f;
+  for (int64_t i = 0; i < n; ++i) {
+    const float* p = pts + 3 * i;
+    const float* q = nrm + 3 * i;
+    const float r = rad[i];
+    if (!finite3(p) || !finite3(q) || !std::isfinite(r) || !(r > 0.0f))
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
+                       "disc " + std::to_string(i) + ": non-finite value or radius <= 0");
+    const float l2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+    if (!(std::fabs(std::sqrt(l2) - 1.0f) <= 1e-3f))
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "disc " + std::to_string(i) + ": normal is not unit length");
+    cr[(size_t)i] = make_float4(p[0], p[1], p[2], r);
+    nn[(size_t)i] = make_float4(q[0], q[1], q[2], 0.0f);
+    for (int a = 0; a < 3; ++a) {
+      cmin[a] = std::min(cmin[a], p[a]);
+      cmax[a] = std::max(cmax[a], p[a]);
+    }
+    rmax = std::max(rmax, r);
+  }
+  if (!rebuild && n != g.nd)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "update_discs: the disc count must not change");
+  g.nd = n;
+  for (int a = 0; a < 3; ++a) {
+    g.cmin[a] = cmin[a];
+    g.cmax[a] = cmax[a];
+  }
+  g.rmax = rmax;
+  RTG_TRY(dalloc(ctx, g.disc_cr_by_id, (size_t)(n > 0 ? n : 1), "discs"));
+  RTG_TRY(dalloc(ctx, g.disc_n_by_id, (size_t)(n > 0 ? n : 1), "disc normals"));
+  if (n > 0) {
+    RTG_CUDA(ctx, cudaMemcpyAsync(g.disc_cr_by_id.p, cr.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    RTG_CUDA(ctx, cudaMemcpyAsync(g.disc_n_by_id.p, nn.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  }
+  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RTG_OK;
+}
+
+int upload_triangles_impl(rtg_context* ctx, const float* vertices, const uint32_t* indices, int64_t nv,
+                          int64_t nt) {
+  if (nv < 0 || nt < 0 || (nt > 0 && (!vertices || !indices)))
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "triangles: null array or negative count");
+  Geometry& g = ctx->g;
+  std::vector<float4> v((size_t)nv);
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int64_t i = 0; i < nv; ++i) {
+    if (!finite3(vertices + 3 * i))
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "vertex " + std::to_string(i) + " is not finite");
+    v[(size_t)i] = make_float4(vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2], 0.0f);
+  }
+  for (int64_t t = 0; t < nt; ++t)
+    for (int k = 0; k < 3; ++k) {
+      const uint32_t idx = indices[3 * t + k];
+      if ((int64_t)idx >= nv)
+        return set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
+                         "triangle " + std::to_string(t) + ": vertex index out of range");
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(lo[a], vertices[3 * (int64_t)idx + a]);
+        hi[a] = std::max(hi[a], vertices[3 * (int64_t)idx + a]);
+      }
+    }
+  g.nt = nt;
+  g.nv = nv;
+  for (int a = 0; a < 3; ++a) {
+    g.tri_min[a] = lo[a];
+    g.tri_max[a] = hi[a];
+  }
+  RTG_TRY(dalloc(ctx, g.tri_v, (size_t)(nv > 0 ? nv : 1), "vertices"));
+  RTG_TRY(dalloc(ctx, g.tri_idx, (size_t)(3 * (nt > 0 ? nt : 1)), "triangle indices"));
+  if (nv > 0)
+    RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_v.p, v.data(), nv * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+  if (nt > 0)
+    RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_idx.p, indices, 3 * nt * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RTG_OK;
+}
+
+int rebuild_all(rtg_context* ctx) {
+  RTG_TRY(build_lbvh(ctx));
+  RTG_TRY(build_neighbors(ctx));
+  RTG_TRY(alloc_results(ctx));
+  resolve_box(ctx);
+  return RTG_OK;
+}
+
+}  // namespace
+}  // namespace rtg
+
+using namespace rtg;
+
+extern "C" {
+
+int rtg_abi_version(void) { return RTG_ABI_VERSION; }
+
+void rtg_config_default(rtg_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof *c);
+  c->x_bound = RTG_BOUND_REFLECTIVE;
+  c->y_bound = RTG_BOUND_REFLECTIVE;
+  c->reflection = RTG_REFLECT_DIFFUSE;
+  c->specular_fraction = 0.0f;
+  c->sticking = 1.0f;
+  c->source_exponent = 1.0f;
+  c->box_mode = RTG_BOX_FROM_GEOMETRY;
+  c->tnear = 1e-4f;
+  c->roulette_threshold = 0.1;
+  c->roulette_weight = 0.3;
+  c->max_segments = 1u << 16;
+  c->job = 0;
+}
+
+int rtg_create(rtg_context** out, int device) {
+  if (!out) return RTG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return RTG_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = new rtg_context();
+  ctx->device = device;
+  rtg_config_default(&ctx->cfg);
+  int rc = RTG_OK;
+  do {
+    if ((rc = use_device(ctx)) != RTG_OK) break;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = RTG_ERR_CUDA; break; }
+    if (cudaMalloc((void**)&ctx->d_tally, sizeof(DevTally)) != cudaSuccess) { rc = RTG_ERR_OUT_OF_MEMORY; break; }
+    if (cudaHostAlloc((void**)&ctx->h_abort, sizeof(uint32_t), cudaHostAllocMapped) != cudaSuccess) {
+      rc = RTG_ERR_CUDA;
+      break;
+    }
+    *ctx->h_abort = 0;
+    if (cudaHostGetDevicePointer((void**)&ctx->d_abort, ctx->h_abort, 0) != cudaSuccess) { rc = RTG_ERR_CUDA; break; }
+    if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        cudaEventCreate(&ctx->evk0) != cudaSuccess || cudaEventCreate(&ctx->evk1) != cudaSuccess) {
+      rc = RTG_ERR_CUDA;
+      break;
+    }
+    cudaMemset(ctx->d_tally, 0, sizeof(DevTally));
+  } while (0);
+  if (rc != RTG_OK) {
+    cudaGetLastError();
+    rtg_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return RTG_OK;
+}
+
+int rtg_destroy(rtg_context* ctx) {
+  if (!ctx) return RTG_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  Geometry& g = ctx->g;
+  dfree(g.disc_cr_by_id); dfree(g.disc_n_by_id); dfree(g.tri_v); dfree(g.tri_idx);
+  dfree(g.disc_cr); dfree(g.disc_n); dfree(g.tri); dfree(g.tri_n); dfree(g.nodes);
+  dfree(g.leaf_ref); dfree(g.leaf_prim); dfree(g.parent); dfree(g.prim_lo); dfree(g.prim_hi);
+  dfree(g.refit_flags); dfree(g.nb_ptr); dfree(g.nb_idx);
+  dfree(ctx->sticking_field); dfree(ctx->acc); dfree(ctx->cnt); dfree(ctx->areas); dfree(ctx->est);
+  dfree(ctx->stat_tmp);
+  if (ctx->d_tally) cudaFree(ctx->d_tally);
+  if (ctx->h_abort) cudaFreeHost(ctx->h_abort);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->evk0) cudaEventDestroy(ctx->evk0);
+  if (ctx->evk1) cudaEventDestroy(ctx->evk1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return RTG_OK;
+}
+
+const char* rtg_last_error(const rtg_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int rtg_upload_mixed(rtg_context* ctx, const float* points, const float* normals, const float* radii, int64_t nd,
+                     const float* vertices, const uint32_t* indices, int64_t nv, int64_t nt) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  RTG_TRY(upload_discs_impl(ctx, points, normals, radii, nd, true));
+  RTG_TRY(upload_triangles_impl(ctx, vertices, indices, nv, nt));
+  if (ctx->g.nd + ctx->g.nt == 0) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no primitives");
+  dfree(ctx->sticking_field);
+  return rebuild_all(ctx);
+}
+
+int rtg_upload_discs(rtg_context* ctx, const float* points, const float* normals, const float* radii, int64_t n) {
+  return rtg_upload_mixed(ctx, points, normals, radii, n, nullptr, nullptr, 0, 0);
+}
+
+int rtg_upload_triangles(rtg_context* ctx, const float* vertices, const uint32_t* indices, int64_t nv, int64_t nt) {
+  return rtg_upload_mixed(ctx, nullptr, nullptr, nullptr, 0, vertices, indices, nv, nt);
+}
+
+int rtg_update_discs(rtg_context* ctx, const float* points, const float* normals, const float* radii, int64_t n) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (ctx->g.nd == 0 || !ctx->g.nodes.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no discs to update");
+  RTG_TRY(use_device(ctx));
+  RTG_TRY(upload_discs_impl(ctx, points, normals, radii, n, false));
+  RTG_TRY(refit_lbvh(ctx));
+  RTG_TRY(build_neighbors(ctx));
+  RTG_TRY(alloc_results(ctx));
+  resolve_box(ctx);
+  return RTG_OK;
+}
+
+int rtg_update_vertices(rtg_context* ctx, const float* vertices, int64_t nv) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  Geometry& g = ctx->g;
+  if (g.nt == 0 || nv != g.nv || !vertices)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "update_vertices: vertex count must match the upload");
+  RTG_TRY(use_device(ctx));
+  std::vector<float4> v((size_t)nv);
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int64_t i = 0; i < nv; ++i) {
+    if (!finite3(vertices + 3 * i)) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "vertex is not finite");
+    v[(size_t)i] = make_float4(vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2], 0.0f);
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], vertices[3 * i + a]);
+      hi[a] = std::max(hi[a], vertices[3 * i + a]);
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    g.tri_min[a] = lo[a];
+    g.tri_max[a] = hi[a];
+  }
+  RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_v.p, v.data(), nv * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+  RTG_TRY(refit_lbvh(ctx));
+  RTG_TRY(alloc_results(ctx));
+  resolve_box(ctx);
+  return RTG_OK;
+}
+
+int rtg_set_config(rtg_context* ctx, const rtg_config* cfg) {
+  if (!ctx || !cfg) return RTG_ERR_INVALID_ARGUMENT;
+  const rtg_config& c = *cfg;
+  auto bad = [&](const char* m) { return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, m); };
+  if ((c.x_bound != RTG_BOUND_REFLECTIVE && c.x_bound != RTG_BOUND_PERIODIC) ||
+      (c.y_bound != RTG_BOUND_REFLECTIVE && c.y_bound != RTG_BOUND_PERIODIC))
+    return bad("bound condition must be RTG_BOUND_REFLECTIVE or RTG_BOUND_PERIODIC");
+  if (c.reflection < RTG_REFLECT_DIFFUSE || c.reflection > RTG_REFLECT_MIXED) return bad("unknown reflection");
+  if (!(c.specular_fraction >= 0.0f && c.specular_fraction <= 1.0f)) return bad("specular_fraction not in [0,1]");
+  if (!(c.sticking >= 0.0f && c.sticking <= 1.0f)) return bad("sticking not in [0,1]");
+  if (!(c.source_exponent >= 0.0f) || !std::isfinite(c.source_exponent)) return bad("source_exponent must be >= 0");
+  if (!(c.tnear >= 0.0f) || !std::isfinite(c.tnear)) return bad("tnear must be >= 0");
+  if (!(c.roulette_threshold >= 0.0 && c.roulette_threshold <= c.roulette_weight && c.roulette_weight <= 1.0))
+    return bad("roulette needs 0 <= threshold <= weight <= 1");
+  if (c.max_segments == 0) return bad("max_segments must be > 0");
+  if (c.box_mode != RTG_BOX_FROM_GEOMETRY && c.box_mode != RTG_BOX_EXPLICIT) return bad("unknown box_mode");
+  if (c.box_mode == RTG_BOX_EXPLICIT) {
+    for (int a = 0; a < 3; ++a)
+      if (!(c.box_lo[a] < c.box_hi[a]) || !std::isfinite(c.box_lo[a]) || !std::isfinite(c.box_hi[a]))
+        return bad("explicit box needs finite box_lo < box_hi");
+  }
+  ctx->cfg = c;
+  resolve_box(ctx);
+  return RTG_OK;
+}
+
+int rtg_get_config(const rtg_context* ctx, rtg_config* cfg) {
+  if (!ctx || !cfg) return RTG_ERR_INVALID_ARGUMENT;
+  *cfg = ctx->cfg;
+  return RTG_OK;
+}
+
+int rtg_get_box(const rtg_context* ctx, float* lo, float* hi) {
+  if (!ctx || !lo || !hi) return RTG_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = ctx->box_lo[a];
+    hi[a] = ctx->box_hi[a];
+  }
+  return RTG_OK;
+}
+
+int rtg_set_sticking(rtg_context* ctx, float s) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (!(s >= 0.0f && s <= 1.0f)) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "sticking not in [0,1]");
+  ctx->cfg.sticking = s;
+  return RTG_OK;
+}
+
+int rtg_set_sticking_field(rtg_context* ctx, const float* s, int64_t n) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  if (!s) {
+    dfree(ctx->sticking_field);
+    return RTG_OK;
+  }
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  if (n != np) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "sticking field length != number of primitives");
+  for (int64_t i = 0; i < n; ++i)
+    if (!(s[i] >= 0.0f && s[i] <= 1.0f))
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "sticking field value not in [0,1]");
+  RTG_TRY(dalloc(ctx, ctx->sticking_field, (size_t)n, "sticking field"));
+  RTG_CUDA(ctx, cudaMemcpyAsync(ctx->sticking_field.p, s, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RTG_OK;
+}
+
+int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, int accumulate,
+                    void* stream) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (ray_end < ray_begin) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "ray_end < ray_begin");
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  if (np == 0 || !ctx->g.nodes.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no geometry uploaded");
+  RTG_TRY(use_device(ctx));
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const rtg_config& c = ctx->cfg;
+  for (int a = 0; a < 3; ++a)
+    if (!(ctx->box_lo[a] < ctx->box_hi[a]) && a < 2)
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "degenerate x/y box (all discs on one line?)");
+  *ctx->h_abort = 0;
+  TraceParams p{};
+  p.s = scene_view(ctx);
+  p.s1 = ctx->acc.p;
+  p.s2 = ctx->acc.p + np;
+  p.s3 = ctx->acc.p + 2 * np;
+  p.s4 = ctx->acc.p + 3 * np;
+  p.cnt = ctx->cnt.p;
+  p.tally = ctx->d_tally;
+  p.abort_flag = ctx->d_abort;
+  p.ray_begin = ray_begin;
+  p.ray_end = ray_end;
+  p.seed = seed;
+  for (int a = 0; a < 3; ++a) {
+    p.box_lo[a] = ctx->box_lo[a];
+    p.box_hi[a] = ctx->box_hi[a];
+  }
+  p.src_lo[0] = ctx->box_lo[0];
+  p.src_lo[1] = ctx->box_lo[1];
+  p.src_hi[0] = ctx->box_hi[0];
+  p.src_hi[1] = ctx->box_hi[1];
+  p.tnear = c.tnear;
+  p.sticking = c.sticking;
+  p.source_exponent = c.source_exponent;
+  p.source_ee = 2.0f / (c.source_exponent + 1.0f);
+  p.specular_fraction = c.specular_fraction;
+  p.roulette_threshold = c.roulette_threshold;
+  p.roulette_weight = c.roulette_weight;
+  p.x_periodic = c.x_bound == RTG_BOUND_PERIODIC;
+  p.y_periodic = c.y_bound == RTG_BOUND_PERIODIC;
+  p.reflection = c.reflection;
+  p.max_segments = c.max_segments;
+  p.job = c.job;
+  RTG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  if (!accumulate) {
+    RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * np * sizeof(double), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(ctx->cnt.p, 0, np * sizeof(unsigned long long), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
+    ctx->last_rays = 0;
+  } else {
+    RTG_CUDA(ctx, cudaMemsetAsync(&ctx->d_tally->next_ray, 0, sizeof(unsigned long long), st));
+  }
+  RTG_CUDA(ctx, cudaEventRecord(ctx->evk0, st));
+  if (ray_end > ray_begin) RTG_TRY(launch_trace(ctx, p, st));
+  RTG_CUDA(ctx, cudaEventRecord(ctx->evk1, st));
+  RTG_TRY(compute_areas(ctx, st, ctx->box_lo, ctx->box_hi));
+  RTG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  ctx->last_rays += ray_end - ray_begin;
+  ctx->traced = true;
+  ctx->finalized = false;
+  return RTG_OK;
+}
+
+int rtg_trace(rtg_context* ctx, uint64_t n_rays, uint64_t seed, void* stream) {
+  return rtg_trace_range(ctx, 0, n_rays, seed, 0, stream);
+}
+
+int rtg_synchronize(rtg_context* ctx) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  RTG_CUDA(ctx, cudaDeviceSynchronize());
+  return RTG_OK;
+}
+
+int rtg_request_abort(rtg_context* ctx) {
+  if (!ctx || !ctx->h_abort) return RTG_ERR_INVALID_ARGUMENT;
+  *(volatile uint32_t*)ctx->h_abort = 1u;
+  return RTG_OK;
+}
+
+int rtg_trace_rays(rtg_context* ctx, const float* rays, int64_t n, float tnear, int32_t* prim_out, float* t_out) {
+  if (!ctx || n < 0 || (n > 0 && (!rays || !prim_out || !t_out))) return RTG_ERR_INVALID_ARGUMENT;
+  if (ctx->g.nd + ctx->g.nt == 0 || !ctx->g.nodes.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no geometry");
+  if (n == 0) return RTG_OK;
+  RTG_TRY(use_device(ctx));
+  DBuf<float> dr, dt;
+  DBuf<int32_t> dp;
+  int rc = dalloc(ctx, dr, (size_t)(6 * n), "rays");
+  if (rc == RTG_OK) rc = dalloc(ctx, dt, (size_t)n, "ray t");
+  if (rc == RTG_OK) rc = dalloc(ctx, dp, (size_t)n, "ray prim");
+  if (rc == RTG_OK) {
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(dr.p, rays, 6 * n * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&ctx->d_tally->errors, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) rc = check_cuda(ctx, e, "trace_rays upload");
+    if (rc == RTG_OK) rc = launch_closest_hit(ctx, dr.p, n, tnear, dp.p, dt.p, st);
+    if (rc == RTG_OK) {
+      e = cudaMemcpyAsync(prim_out, dp.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, dt.p, n * sizeof(float), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) rc = check_cuda(ctx, e, "trace_rays");
+    }
+  }
+  dfree(dr);
+  dfree(dt);
+  dfree(dp);
+  return rc;
+}
+
+int rtg_num_primitives(const rtg_context* ctx, int64_t* n) {
+  if (!ctx || !n) return RTG_ERR_INVALID_ARGUMENT;
+  *n = ctx->g.nd + ctx->g.nt;
+  return RTG_OK;
+}
+
+static int sync_trace(rtg_context* ctx) {
+  RTG_TRY(use_device(ctx));
+  RTG_CUDA(ctx, cudaDeviceSynchronize());
+  DevTally t;
+  RTG_CUDA(ctx, cudaMemcpy(&t, ctx->d_tally, sizeof t, cudaMemcpyDeviceToHost));
+  if (t.abort_seen) return set_error(ctx, RTG_ERR_ABORTED, "trace aborted on request");
+  if (t.errors) return set_error(ctx, RTG_ERR_BUDGET, "a device-side traversal limit was reached");
+  return RTG_OK;
+}
+
+int rtg_get_mc_estimates(rtg_context* ctx, float* out) {
+  if (!ctx || !out) return RTG_ERR_INVALID_ARGUMENT;
+  if (!ctx->traced) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "no trace has run");
+  RTG_TRY(sync_trace(ctx));
+  if (!ctx->finalized) {
+    RTG_TRY(finalize_estimates(ctx, ctx->stream));
+    ctx->finalized = true;
+  }
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  RTG_CUDA(ctx, cudaMemcpy(out, ctx->est.p, np * sizeof(float), cudaMemcpyDeviceToHost));
+  return RTG_OK;
+}
+
+int rtg_get_hit_counts(rtg_context* ctx, uint64_t* out) {
+  if (!ctx || !out) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(sync_trace(ctx));
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  RTG_CUDA(ctx, cudaMemcpy(out, ctx->cnt.p, np * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  return RTG_OK;
+}
+
+int rtg_get_accumulators(rtg_context* ctx, double* s1, double* s2, double* s3, double* s4) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(sync_trace(ctx));
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  double* outs[4] = {s1, s2, s3, s4};
+  for (int k = 0; k < 4; ++k)
+    if (outs[k]) RTG_CUDA(ctx, cudaMemcpy(outs[k], ctx->acc.p + k * np, np * sizeof(double), cudaMemcpyDeviceToHost));
+  return RTG_OK;
+}
+
+int rtg_get_exposed_areas(rtg_context* ctx, float* out) {
+  if (!ctx || !out) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  if (!ctx->traced) {
+    RTG_TRY(compute_areas(ctx, ctx->stream, ctx->box_lo, ctx->box_hi));
+  }
+  RTG_CUDA(ctx, cudaDeviceSynchronize());
+  RTG_CUDA(ctx, cudaMemcpy(out, ctx->areas.p, np * sizeof(float), cudaMemcpyDeviceToHost));
+  return RTG_OK;
+}
+
+static int stats_to_host(rtg_context* ctx, double* out, bool vov) {
+  RTG_TRY(sync_trace(ctx));
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  DevTally t;
+  RTG_CUDA(ctx, cudaMemcpy(&t, ctx->d_tally, sizeof t, cudaMemcpyDeviceToHost));
+  RTG_TRY(dalloc(ctx, ctx->stat_tmp, (size_t)(2 * np), "statistics"));
+  RTG_TRY(compute_stats(ctx, ctx->stream, t.total, ctx->stat_tmp.p, ctx->stat_tmp.p + np));
+  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  RTG_CUDA(ctx, cudaMemcpy(out, ctx->stat_tmp.p + (vov ? np : 0), np * sizeof(double), cudaMemcpyDeviceToHost));
+  return RTG_OK;
+}
+
+int rtg_get_relative_error(rtg_context* ctx, double* out) {
+  if (!ctx || !out) return RTG_ERR_INVALID_ARGUMENT;
+  return stats_to_host(ctx, out, false);
+}
+
+int rtg_get_vov(rtg_context* ctx, double* out) {
+  if (!ctx || !out) return RTG_ERR_INVALID_ARGUMENT;
+  return stats_to_host(ctx, out, true);
+}
+
+int rtg_get_tally(rtg_context* ctx, rtg_tally* out) {
+  if (!ctx || !out) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  RTG_CUDA(ctx, cudaDeviceSynchronize());
+  DevTally t;
+  RTG_CUDA(ctx, cudaMemcpy(&t, ctx->d_tally, sizeof t, cudaMemcpyDeviceToHost));
+  std::memset(out, 0, sizeof *out);
+  out->num_rays = ctx->last_rays;
+  out->hitc = t.hitc;
+  out->nonhitc = t.nonhitc;
+  out->total = t.total;
+  out->segments = t.segments;
+  out->truncated = t.truncated;
+  out->nb_deposits = t.nb_deposits;
+  out->errors = t.errors;
+  float ms = 0.0f;
+  if (ctx->traced && cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) out->trace_ms = ms;
+  if (ctx->traced && cudaEventElapsedTime(&ms, ctx->evk0, ctx->evk1) == cudaSuccess) out->kernel_ms = ms;
+  cudaGetLastError();
+  return RTG_OK;
+}
+
+int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols, int64_t cap, int64_t* nnz) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  const int64_t nd = ctx->g.nd;
+  if (nnz) *nnz = ctx->g.nb_nnz;
+  if (row_ptr && nd > 0)
+    RTG_CUDA(ctx, cudaMemcpy(row_ptr, ctx->g.nb_ptr.p, (nd + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  if (cols) {
+    if (cap < ctx->g.nb_nnz) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "neighbour buffer too small");
+    if (ctx->g.nb_nnz > 0)
+      RTG_CUDA(ctx, cudaMemcpy(cols, ctx->g.nb_idx.p, ctx->g.nb_nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  }
+  return RTG_OK;
+}
+
+int rtg_get_device_view(rtg_context* ctx, rtg_device_view* v) {
+  if (!ctx || !v) return RTG_ERR_INVALID_ARGUMENT;
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  v->s1 = ctx->acc.p;
+  v->s2 = ctx->acc.p ? ctx->acc.p + np : nullptr;
+  v->s3 = ctx->acc.p ? ctx->acc.p + 2 * np : nullptr;
+  v->s4 = ctx->acc.p ? ctx->acc.p + 3 * np : nullptr;
+  v->counts = (uint64_t*)ctx->cnt.p;
+  v->areas = ctx->areas.p;
+  v->estimates = ctx->est.p;
+  v->n = np;
+  return RTG_OK;
+}
+
+int rtg_device_run(const float* points, const float* normals, const float* radii, int64_t n, const rtg_config* cfg,
+                   const float* sticking_field, uint64_t n_rays, uint64_t seed, float* est_out, uint64_t* cnt_out,
+                   int device) {
+  rtg_context* ctx = nullptr;
+  int rc = rtg_create(&ctx, device);
+  if (rc != RTG_OK) return rc;
+  rtg_config c;
+  if (cfg) c = *cfg;
+  else rtg_config_default(&c);
+  do {
+    if ((rc = rtg_upload_discs(ctx, points, normals, radii, n)) != RTG_OK) break;
+    if ((rc = rtg_set_config(ctx, &c)) != RTG_OK) break;
+    if (sticking_field && (rc = rtg_set_sticking_field(ctx, sticking_field, n)) != RTG_OK) break;
+    if ((rc = rtg_trace(ctx, n_rays, seed, nullptr)) != RTG_OK) break;
+    if (est_out && (rc = rtg_get_mc_estimates(ctx, est_out)) != RTG_OK) break;
+    if (cnt_out && (rc = rtg_get_hit_counts(ctx, cnt_out)) != RTG_OK) break;
+  } while (0);
+  rtg_destroy(ctx);
+  return rc;
+}
+
+}  // extern "C"

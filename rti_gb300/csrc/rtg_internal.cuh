@@ -1,0 +1,203 @@
+// rtg_internal.cuh -- context and cross-file declarations of librtg.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/rtg.h"
+
+namespace rtg {
+
+// A BVH child reference: bit 31 = leaf, bit 30 = triangle leaf, bits 0..29 =
+// internal node index or primitive slot.
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kTriBit = 0x40000000u;
+constexpr uint32_t kSlotMask = 0x3FFFFFFFu;
+constexpr int kStackSize = 64;
+
+// One internal node: the boxes of both children and their references (64 B).
+//   a = (c0.lo.x, c0.hi.x, c1.lo.x, c1.hi.x)
+//   b = (c0.lo.y, c0.hi.y, c1.lo.y, c1.hi.y)
+//   c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   d = (child0, child1, parent, unused) as uint32 bits
+struct __align__(16) Node {
+  float4 a, b, c;
+  uint4 d;
+};
+
+// Device status counters (accumulated over a trace).
+struct DevTally {
+  unsigned long long hitc, nonhitc, total, segments, truncated, nb_deposits, errors, next_ray;
+  unsigned int abort_seen;
+  unsigned int pad;
+};
+
+// Read-only view of a scene for the kernels.
+struct SceneView {
+  // discs in LBVH (slot) order: centre + radius, normal + original id bits
+  const float4* disc_cr;
+  const float4* disc_n;
+  int32_t nd;
+  // triangles in slot order: v0 + original id bits, e1, e2 (3 float4 per slot)
+  const float4* tri;
+  const float4* tri_n;  // unit normal per slot
+  int32_t nt;
+  const Node* nodes;
+  uint32_t root;        // child reference of the root (internal node 0 or a leaf)
+  // neighbour CSR over original disc ids, and disc data by original id
+  const int64_t* nb_ptr;
+  const int32_t* nb_idx;
+  const float4* disc_cr_by_id;
+  const float4* disc_n_by_id;
+  const float* sticking_field;  // by original id or nullptr
+};
+
+struct TraceParams {
+  SceneView s;
+  // accumulators by original primitive id
+  double* s1;
+  double* s2;
+  double* s3;
+  double* s4;
+  unsigned long long* cnt;
+  DevTally* tally;
+  volatile uint32_t* abort_flag;  // host-mapped; nonzero asks the kernel to stop
+  uint64_t ray_begin, ray_end;
+  uint64_t seed;
+  float box_lo[3], box_hi[3];
+  float src_lo[2], src_hi[2];
+  float tnear;
+  float sticking;
+  float source_exponent, source_ee;
+  float specular_fraction;
+  double roulette_threshold, roulette_weight;
+  int32_t x_periodic, y_periodic;
+  int32_t reflection;
+  uint32_t max_segments;
+  uint32_t job;
+};
+
+// ---- device buffers owned by a context ----
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+};
+
+struct Geometry {
+  int64_t nd = 0, nt = 0, nv = 0;
+  // inputs by original id
+  DBuf<float4> disc_cr_by_id, disc_n_by_id;
+  DBuf<float4> tri_v;      // nv vertices (xyz, 0)
+  DBuf<uint32_t> tri_idx;  // nt*3
+  // slot-ordered copies
+  DBuf<float4> disc_cr, disc_n, tri, tri_n;
+  DBuf<Node> nodes;
+  DBuf<uint32_t> leaf_ref;    // per sorted leaf i: child reference
+  DBuf<int32_t> leaf_prim;    // per sorted leaf i: original primitive id
+  DBuf<uint32_t> parent;      // parent of internal nodes [0,n-1) and leaves [n-1, 2n-1)
+  DBuf<float> prim_lo, prim_hi;  // per original id, 3 floats each (padded boxes)
+  DBuf<unsigned int> refit_flags;
+  uint32_t root = 0;
+  // neighbours
+  DBuf<int64_t> nb_ptr;
+  DBuf<int32_t> nb_idx;
+  int64_t nb_nnz = 0;
+  // centre extents and max radius (rti's box rule)
+  float cmin[3] = {0, 0, 0}, cmax[3] = {0, 0, 0};
+  float rmax = 0.0f;
+  float tri_min[3] = {0, 0, 0}, tri_max[3] = {0, 0, 0};
+};
+
+}  // namespace rtg
+
+struct rtg_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  rtg_config cfg{};
+  rtg::Geometry g;
+  rtg::DBuf<float> sticking_field;
+  // accumulators (one allocation: s1 | s2 | s3 | s4), counts, areas, estimates
+  rtg::DBuf<double> acc;
+  rtg::DBuf<unsigned long long> cnt;
+  rtg::DBuf<float> areas;
+  rtg::DBuf<float> est;
+  rtg::DBuf<double> stat_tmp;
+  rtg::DevTally* d_tally = nullptr;
+  uint32_t* h_abort = nullptr;  // host-mapped flag
+  uint32_t* d_abort = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  uint64_t last_rays = 0;
+  bool traced = false;
+  bool finalized = false;
+  float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
+  std::string err;
+};
+
+namespace rtg {
+
+// sort.cu
+int exclusive_scan_u32(rtg_context* ctx, uint32_t* d_a, int64_t m, uint32_t* d_total, cudaStream_t st);
+int exclusive_scan_i64(rtg_context* ctx, int64_t* d_a, int64_t m, int64_t* d_total, cudaStream_t st);
+int radix_sort_pairs(rtg_context* ctx, uint32_t* d_keys, uint32_t* d_vals, uint32_t* d_tmp_keys,
+                     uint32_t* d_tmp_vals, int64_t n, int bits, cudaStream_t st);
+// lbvh.cu
+int build_lbvh(rtg_context* ctx);      // full build from the by-id primitive data
+int refit_lbvh(rtg_context* ctx);      // recompute boxes, keep topology
+// surface.cu
+int build_neighbors(rtg_context* ctx);
+int compute_areas(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi);
+int finalize_estimates(rtg_context* ctx, cudaStream_t st);
+int compute_stats(rtg_context* ctx, cudaStream_t st, uint64_t total, double* d_rel, double* d_vov);
+// trace.cu
+int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st);
+int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim,
+                       float* d_t, cudaStream_t st);
+SceneView scene_view(rtg_context* ctx);
+
+// api.cu helpers
+int set_error(rtg_context* ctx, int code, const std::string& msg);
+int check_cuda(rtg_context* ctx, cudaError_t e, const char* what);
+template <typename T>
+int dalloc(rtg_context* ctx, DBuf<T>& b, size_t n, const char* what) {
+  if (b.p && b.n >= n && n > 0) {
+    b.n = n;
+    return RTG_OK;
+  }
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.n = 0;
+  if (n == 0) return RTG_OK;
+  cudaError_t e = cudaMalloc((void**)&b.p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    cudaGetLastError();
+    return set_error(ctx, RTG_ERR_OUT_OF_MEMORY, std::string("cudaMalloc failed for ") + what);
+  }
+  b.n = n;
+  return RTG_OK;
+}
+template <typename T>
+void dfree(DBuf<T>& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.n = 0;
+}
+
+// device helpers shared by the kernels
+__host__ __device__ inline int num_sms_hint() { return 152; }
+
+}  // namespace rtg
+
+#define RTG_CUDA(ctx, call)                                              \
+  do {                                                                   \
+    cudaError_t e__ = (call);                                            \
+    if (e__ != cudaSuccess) return rtg::check_cuda((ctx), e__, #call);   \
+  } while (0)
+
+#define RTG_TRY(expr)            \
+  do {                           \
+    int r__ = (expr);            \
+    if (r__ != RTG_OK) return r__; \
+  } while (0)

@@ -1,0 +1,379 @@
+// rtg_trace.cu -- persistent path-tracing kernel and explicit-ray closest hit.
+//
+// One thread carries one particle path at a time, as tracer::run does per
+// OpenMP iteration (tracer.hpp:160-280): source ray, closest hit, periodic or
+// reflective x/y box, back-face pass-through, sticking deposit on the hit
+// primitive and on every crossed overlapping neighbour disc, Russian
+// roulette, diffuse/specular re-emission.  Threads are persistent: when a
+// lane's path ends it takes the next source-ray id from a global counter
+// (warp-aggregated), so long and short paths share the SIMD lanes.
+//
+// Closest hit = stack traversal of the two-box LBVH nodes; ties in t go to the
+// lower primitive id, and the node boxes are conservative, so the chosen hit
+// does not depend on the traversal order.
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "rtg_internal.cuh"
+#include "rtg_math.cuh"
+
+namespace rtg {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kTraceThreads = 128;
+
+__device__ __forceinline__ float safe_inv(float d) {
+  if (fabsf(d) < 1e-30f) d = d < 0.0f ? -1e-30f : 1e-30f;
+  return 1.0f / d;
+}
+
+struct Ray {
+  f3 o, d, idr;
+};
+
+// Slab test of one child box; returns the entry distance in tn.
+__device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, float lz, float hz, const Ray& r,
+                                     float tmax, float& tn) {
+  float t0x = (lx - r.o.x) * r.idr.x, t1x = (hx - r.o.x) * r.idr.x;
+  float t0y = (ly - r.o.y) * r.idr.y, t1y = (hy - r.o.y) * r.idr.y;
+  float t0z = (lz - r.o.z) * r.idr.z, t1z = (hz - r.o.z) * r.idr.z;
+  tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
+  float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+  return tn <= tf * 1.0000005f && tn <= tmax * 1.0000005f + 1e-30f;
+}
+
+__device__ __forceinline__ void test_leaf(const SceneView& s, uint32_t ref, const Ray& r, float tnear, float& bt,
+                                          int& bid, uint32_t& bref) {
+  const uint32_t slot = ref & kSlotMask;
+  float t;
+  int id;
+  bool h;
+  if (ref & kTriBit) {
+    const float4 a = __ldg(&s.tri[3 * slot]);
+    const float4 b = __ldg(&s.tri[3 * slot + 1]);
+    const float4 c = __ldg(&s.tri[3 * slot + 2]);
+    id = __float_as_int(a.w);
+    h = tri_test(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), r.o, r.d, tnear, t);
+  } else {
+    const float4 cr = __ldg(&s.disc_cr[slot]);
+    const float4 nn = __ldg(&s.disc_n[slot]);
+    id = __float_as_int(nn.w);
+    h = disc_test(mk3(cr.x, cr.y, cr.z), cr.w, mk3(nn.x, nn.y, nn.z), r.o, r.d, tnear, t);
+  }
+  if (h && (t < bt || (t == bt && id < bid))) {
+    bt = t;
+    bid = id;
+    bref = ref;
+  }
+}
+
+// Closest primitive hit; returns false when nothing is hit.  errs counts
+// stack overflows and iteration-limit trips (both end the query).
+__device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& bt, int& bid, uint32_t& bref,
+                            unsigned long long& errs) {
+  Ray r;
+  r.o = o;
+  r.d = d;
+  r.idr = mk3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+  bt = FLT_MAX;
+  bid = INT_MAX;
+  bref = 0xFFFFFFFFu;
+  uint32_t stack[kStackSize];
+  int sp = 0;
+  uint32_t cur = s.root;
+  const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
+  for (int64_t it = 0;; ++it) {
+    if (it > max_iter) {
+      errs += 1;
+      break;
+    }
+    const Node* nd = s.nodes + cur;
+    const float4 a = __ldg(&nd->a);
+    const float4 b = __ldg(&nd->b);
+    const float4 c = __ldg(&nd->c);
+    const uint4 ch = __ldg(&nd->d);
+    float tn0, tn1;
+    bool h0 = slab(a.x, a.y, b.x, b.y, c.x, c.y, r, bt, tn0);
+    bool h1 = slab(a.z, a.w, b.z, b.w, c.z, c.w, r, bt, tn1);
+    if (h0 && (ch.x & kLeafBit)) {
+      test_leaf(s, ch.x, r, tnear, bt, bid, bref);
+      h0 = false;
+    }
+    if (h1 && (ch.y & kLeafBit)) {
+      test_leaf(s, ch.y, r, tnear, bt, bid, bref);
+      h1 = false;
+    }
+    if (h0 && h1) {
+      uint32_t nearc = tn0 <= tn1 ? ch.x : ch.y;
+      uint32_t farc = tn0 <= tn1 ? ch.y : ch.x;
+      if (sp < kStackSize) {
+        stack[sp++] = farc;
+      } else {
+        errs += 1;
+      }
+      cur = nearc;
+    } else if (h0) {
+      cur = ch.x;
+    } else if (h1) {
+      cur = ch.y;
+    } else {
+      if (sp == 0) break;
+      cur = stack[--sp];
+    }
+  }
+  return bid != INT_MAX;
+}
+
+// Side-face exit of the x/y box: 0 = x face, 1 = y face, -1 = the ray leaves
+// through the top or bottom first (a miss).
+__device__ __forceinline__ int boundary_exit(const TraceParams& p, f3 o, f3 d, float& tb) {
+  float tx = FLT_MAX, ty = FLT_MAX, tz = FLT_MAX;
+  if (d.x > 0.0f) tx = (p.box_hi[0] - o.x) / d.x;
+  else if (d.x < 0.0f) tx = (p.box_lo[0] - o.x) / d.x;
+  if (d.y > 0.0f) ty = (p.box_hi[1] - o.y) / d.y;
+  else if (d.y < 0.0f) ty = (p.box_lo[1] - o.y) / d.y;
+  if (d.z > 0.0f) tz = (p.box_hi[2] - o.z) / d.z;
+  else if (d.z < 0.0f) tz = (p.box_lo[2] - o.z) / d.z;
+  const int axis = tx <= ty ? 0 : 1;
+  const float t = tx <= ty ? tx : ty;
+  if (!(t < FLT_MAX)) return -1;
+  if (!(t >= p.tnear)) return -1;
+  if (t > tz) return -1;
+  tb = t;
+  return axis;
+}
+
+// hit_accumulator::use (hit_accumulator.hpp:128-138)
+__device__ __forceinline__ void deposit(const TraceParams& p, int id, float v) {
+  const double dv = (double)v;
+  atomicAdd(&p.s1[id], dv);
+  atomicAdd(&p.s2[id], dv * v);
+  atomicAdd(&p.s3[id], dv * v * v);
+  atomicAdd(&p.s4[id], dv * v * v * v);
+  atomicAdd(&p.cnt[id], 1ull);
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceParams p) {
+  const SceneView& s = p.s;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  unsigned long long c_hit = 0, c_non = 0, c_tot = 0, c_seg = 0, c_trunc = 0, c_nb = 0, c_err = 0;
+  bool active = false, exhausted = false;
+  uint64_t id = 0;
+  f3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
+  float w = 1.0f;
+  uint32_t k = 0, nseg = 0;
+  const uint64_t nrays = p.ray_end - p.ray_begin;
+  const double lower = p.roulette_threshold * 1.0f;
+  const double renew = p.roulette_weight * 1.0f;
+  for (uint32_t iter = 0;; ++iter) {
+    if (!exhausted) {
+      const unsigned need = __ballot_sync(kFull, !active);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&p.tally->next_ray, (unsigned long long)__popc(need));
+        base = __shfl_sync(kFull, base, leader);
+        if (base + __popc(need) >= nrays) exhausted = true;
+        if (!active) {
+          const uint64_t j = base + (uint64_t)__popc(need & lt_mask);
+          if (j < nrays) {
+            id = p.ray_begin + j;
+            // source.hpp:20-58 with rectangle_origin_z / (power_)cosine_direction_z
+            const uint4 u = draw4(p.seed, id, 0xFFFFFFFFu, p.job);
+            const float r1 = u01_co(u.x), r2 = u01_co(u.y);
+            o = mk3(p.src_lo[0] + (p.src_hi[0] - p.src_lo[0]) * r1,
+                    p.src_lo[1] + (p.src_hi[1] - p.src_lo[1]) * r2, p.box_hi[2]);
+            d = source_dir(p.source_exponent, p.source_ee, u.z, u.w);
+            w = 1.0f;
+            k = 0;
+            nseg = 0;
+            active = true;
+          }
+        }
+      }
+    }
+    if (!__any_sync(kFull, active)) break;
+    if ((iter & 255u) == 0u && p.abort_flag) {
+      unsigned stop = 0;
+      if (lane == 0) stop = *p.abort_flag;
+      stop = __shfl_sync(kFull, stop, 0);
+      if (stop) {
+        if (lane == 0) atomicExch(&p.tally->abort_seen, 1u);
+        break;
+      }
+    }
+    if (!active) continue;
+    // ---- one segment (tracer.hpp:169-279) ----
+    if (nseg == p.max_segments) {
+      c_trunc += 1;
+      active = false;
+      continue;
+    }
+    nseg += 1;
+    c_seg += 1;
+    float th, tb = 0.0f;
+    int hid;
+    uint32_t href;
+    const bool hit = closest_hit(s, o, d, p.tnear, th, hid, href, c_err);
+    const int axis = boundary_exit(p, o, d, tb);
+    if (hit && (axis < 0 || th <= tb)) {
+      float4 nn;
+      if (href & kTriBit) nn = __ldg(&s.tri_n[href & kSlotMask]);
+      else nn = __ldg(&s.disc_n[href & kSlotMask]);
+      const f3 n = mk3(nn.x, nn.y, nn.z);
+      const f3 hp = mk3(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
+      if (d.x * n.x + d.y * n.y + d.z * n.z > 0.0f) {  // back face: pass through (tracer.hpp:216-227)
+        o = hp;
+        continue;
+      }
+      c_hit += 1;
+      const float st = s.sticking_field ? __ldg(&s.sticking_field[hid]) : p.sticking;
+      const float v = w * st;
+      deposit(p, hid, v);
+      c_tot += 1;
+      if (!(href & kTriBit) && s.nb_ptr) {  // tracer.hpp:339-383
+        const int64_t q0 = __ldg(&s.nb_ptr[hid]), q1 = __ldg(&s.nb_ptr[hid + 1]);
+        for (int64_t q = q0; q < q1; ++q) {
+          const int nb = __ldg(&s.nb_idx[q]);
+          const float4 cr = __ldg(&s.disc_cr_by_id[nb]);
+          const float4 nv = __ldg(&s.disc_n_by_id[nb]);
+          if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
+            deposit(p, nb, v);
+            c_tot += 1;
+            c_nb += 1;
+          }
+        }
+      }
+      w = w - v;
+      if (w == 0.0f) {
+        active = false;
+        continue;
+      }
+      const uint4 u = draw4(p.seed, id, k, p.job);
+      // rejection_control::check_weight_reweight_or_kill (rejection_control.hpp:28-61)
+      if (!((double)w >= lower)) {
+        const double kill = 1.0f - (double)w / renew;
+        if ((double)u.x < kill * 4294967296.0) {
+          active = false;
+          continue;
+        }
+        w = (float)renew;
+      }
+      const bool spec = p.reflection == RTG_REFLECT_SPECULAR ||
+                        (p.reflection == RTG_REFLECT_MIXED &&
+                         (double)u.w < (double)p.specular_fraction * 4294967296.0);
+      d = spec ? specular_dir(n, d) : diffuse_dir(n, u.y, u.z);
+      o = hp;
+      k += 1;
+      continue;
+    }
+    if (axis >= 0) {  // boundary_x_y::process_hit (boundary_x_y.hpp:92-143)
+      f3 hp = mk3(o.x + d.x * tb, o.y + d.y * tb, o.z + d.z * tb);
+      const int periodic = axis == 0 ? p.x_periodic : p.y_periodic;
+      if (periodic) {
+        if (axis == 0) hp.x = d.x > 0.0f ? p.box_lo[0] : p.box_hi[0];
+        else hp.y = d.y > 0.0f ? p.box_lo[1] : p.box_hi[1];
+      } else {
+        if (axis == 0) d.x = -d.x;
+        else d.y = -d.y;
+      }
+      o = hp;
+      continue;
+    }
+    c_non += 1;
+    active = false;
+  }
+  c_hit = warp_sum(c_hit);
+  c_non = warp_sum(c_non);
+  c_tot = warp_sum(c_tot);
+  c_seg = warp_sum(c_seg);
+  c_trunc = warp_sum(c_trunc);
+  c_nb = warp_sum(c_nb);
+  c_err = warp_sum(c_err);
+  if (lane == 0) {
+    atomicAdd(&p.tally->hitc, c_hit);
+    atomicAdd(&p.tally->nonhitc, c_non);
+    atomicAdd(&p.tally->total, c_tot);
+    atomicAdd(&p.tally->segments, c_seg);
+    atomicAdd(&p.tally->truncated, c_trunc);
+    atomicAdd(&p.tally->nb_deposits, c_nb);
+    atomicAdd(&p.tally->errors, c_err);
+  }
+}
+
+__global__ void closest_hit_kernel(const SceneView s, const float* __restrict__ rays, int64_t n, float tnear,
+                                   int32_t* __restrict__ prim, float* __restrict__ tout,
+                                   unsigned long long* errors) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* r = rays + 6 * i;
+  float t;
+  int id;
+  uint32_t ref;
+  unsigned long long e = 0;
+  if (closest_hit(s, mk3(r[0], r[1], r[2]), mk3(r[3], r[4], r[5]), tnear, t, id, ref, e)) {
+    prim[i] = id;
+    tout[i] = t;
+  } else {
+    prim[i] = -1;
+    tout[i] = 0.0f;
+  }
+  if (e) atomicAdd(errors, e);
+}
+
+}  // namespace
+
+SceneView scene_view(rtg_context* ctx) {
+  const Geometry& g = ctx->g;
+  SceneView s{};
+  s.disc_cr = g.disc_cr.p;
+  s.disc_n = g.disc_n.p;
+  s.nd = (int32_t)g.nd;
+  s.tri = g.tri.p;
+  s.tri_n = g.tri_n.p;
+  s.nt = (int32_t)g.nt;
+  s.nodes = g.nodes.p;
+  s.root = g.root;
+  s.nb_ptr = g.nd > 0 ? g.nb_ptr.p : nullptr;
+  s.nb_idx = g.nb_idx.p;
+  s.disc_cr_by_id = g.disc_cr_by_id.p;
+  s.disc_n_by_id = g.disc_n_by_id.p;
+  s.sticking_field = ctx->sticking_field.p;
+  return s;
+}
+
+int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st) {
+  int dev = ctx->device, sms = 0, per_sm = 0;
+  RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_paths_kernel, kTraceThreads, 0));
+  if (per_sm < 1) per_sm = 1;
+  uint64_t nrays = p.ray_end - p.ray_begin;
+  uint64_t blocks = (uint64_t)sms * per_sm;
+  uint64_t need = (nrays + kTraceThreads - 1) / kTraceThreads;
+  if (need < blocks) blocks = need > 0 ? need : 1;
+  trace_paths_kernel<<<(unsigned)blocks, kTraceThreads, 0, st>>>(p);
+  RTG_CUDA(ctx, cudaGetLastError());
+  return RTG_OK;
+}
+
+int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim, float* d_t,
+                       cudaStream_t st) {
+  if (n <= 0) return RTG_OK;
+  SceneView s = scene_view(ctx);
+  closest_hit_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, d_rays, n, tnear, d_prim, d_t,
+                                                                   &ctx->d_tally->errors);
+  RTG_CUDA(ctx, cudaGetLastError());
+  return RTG_OK;
+}
+
+}  // namespace rtg

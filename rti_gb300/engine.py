@@ -1,0 +1,246 @@
+"""Engine: one GPU's flux-tracing context (a thin owner of an ``rtg_context``).
+
+Every method calls the C ABI of librtg.so; nothing here computes flux on the
+host.  Arrays are numpy (host) arrays; ``device_view()`` exposes the
+device-resident accumulators for zero-copy use (e.g. torch.distributed).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a.reshape(shape) if shape is not None else a
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+@dataclass
+class Tally:
+    num_rays: int
+    hitc: int
+    nonhitc: int
+    total: int
+    segments: int
+    truncated: int
+    nb_deposits: int
+    errors: int
+    trace_ms: float
+    kernel_ms: float
+
+
+class Engine:
+    """Flux engine on one CUDA device (rti::device + tracer on a GB300)."""
+
+    def __init__(self, device: int = 0):
+        self._L = L.load()
+        self._h = C.c_void_p()
+        rc = self._L.rtg_create(C.byref(self._h), int(device))
+        if rc != L.RTG_OK:
+            raise L.RtgError(rc, "rtg_create failed (no usable CUDA device?)")
+        self.device = device
+        self.n_discs = 0
+        self.n_triangles = 0
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.rtg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != L.RTG_OK:
+            msg = self._L.rtg_last_error(self._h)
+            raise L.RtgError(rc, msg.decode() if msg else "")
+
+    # -- geometry -------------------------------------------------------------
+    def upload_discs(self, points, normals, radii):
+        p = _f32(points, (-1, 3))
+        n = _f32(normals, (-1, 3))
+        r = _f32(radii, (-1,))
+        if not (len(p) == len(n) == len(r)):
+            raise ValueError("points, normals and radii must have the same length")
+        self._check(self._L.rtg_upload_discs(self._h, _ptr(p, L._f32p), _ptr(n, L._f32p), _ptr(r, L._f32p), len(p)))
+        self.n_discs, self.n_triangles = len(p), 0
+
+    def upload_triangles(self, vertices, indices):
+        v = _f32(vertices, (-1, 3))
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+        self._check(self._L.rtg_upload_triangles(self._h, _ptr(v, L._f32p), _ptr(i, L._u32p), len(v), len(i)))
+        self.n_discs, self.n_triangles = 0, len(i)
+
+    def upload_mixed(self, points, normals, radii, vertices, indices):
+        """Discs (ids 0..nd-1) and triangles (ids nd..nd+nt-1) in one surface."""
+        p, n, r = _f32(points, (-1, 3)), _f32(normals, (-1, 3)), _f32(radii, (-1,))
+        v = _f32(vertices, (-1, 3))
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+        self._check(self._L.rtg_upload_mixed(self._h, _ptr(p, L._f32p), _ptr(n, L._f32p), _ptr(r, L._f32p), len(p),
+                                             _ptr(v, L._f32p), _ptr(i, L._u32p), len(v), len(i)))
+        self.n_discs, self.n_triangles = len(p), len(i)
+
+    def update_discs(self, points, normals, radii):
+        p, n, r = _f32(points, (-1, 3)), _f32(normals, (-1, 3)), _f32(radii, (-1,))
+        self._check(self._L.rtg_update_discs(self._h, _ptr(p, L._f32p), _ptr(n, L._f32p), _ptr(r, L._f32p), len(p)))
+
+    def update_vertices(self, vertices):
+        v = _f32(vertices, (-1, 3))
+        self._check(self._L.rtg_update_vertices(self._h, _ptr(v, L._f32p), len(v)))
+
+    @property
+    def num_primitives(self) -> int:
+        n = C.c_int64()
+        self._check(self._L.rtg_num_primitives(self._h, C.byref(n)))
+        return n.value
+
+    # -- configuration --------------------------------------------------------
+    def configure(self, *, x_bound=None, y_bound=None, reflection=None, specular_fraction=None, sticking=None,
+                  source_exponent=None, box=None, tnear=None, roulette_threshold=None, roulette_weight=None,
+                  max_segments=None, job=None):
+        """Updates the trace configuration; ``box`` = ((xlo, ylo, zlo), (xhi, yhi, zhi)) or None for rti's rule."""
+        c = L.RtgConfig()
+        self._check(self._L.rtg_get_config(self._h, C.byref(c)))
+        for name, val in (("x_bound", x_bound), ("y_bound", y_bound), ("reflection", reflection),
+                          ("specular_fraction", specular_fraction), ("sticking", sticking),
+                          ("source_exponent", source_exponent), ("tnear", tnear),
+                          ("roulette_threshold", roulette_threshold), ("roulette_weight", roulette_weight),
+                          ("max_segments", max_segments), ("job", job)):
+            if val is not None:
+                setattr(c, name, val)
+        if box is not None:
+            c.box_mode = L.RTG_BOX_EXPLICIT
+            for a in range(3):
+                c.box_lo[a] = box[0][a]
+                c.box_hi[a] = box[1][a]
+        self._check(self._L.rtg_set_config(self._h, C.byref(c)))
+        return self
+
+    def config(self) -> L.RtgConfig:
+        c = L.RtgConfig()
+        self._check(self._L.rtg_get_config(self._h, C.byref(c)))
+        return c
+
+    def box(self):
+        lo = np.zeros(3, dtype=np.float32)
+        hi = np.zeros(3, dtype=np.float32)
+        self._check(self._L.rtg_get_box(self._h, _ptr(lo, L._f32p), _ptr(hi, L._f32p)))
+        return lo, hi
+
+    def set_sticking_field(self, field):
+        if field is None:
+            self._check(self._L.rtg_set_sticking_field(self._h, None, 0))
+            return
+        f = _f32(field, (-1,))
+        self._check(self._L.rtg_set_sticking_field(self._h, _ptr(f, L._f32p), len(f)))
+
+    # -- tracing --------------------------------------------------------------
+    def trace(self, n_rays: int, seed: int = 0, stream=None, *, ray_begin: int = 0, accumulate: bool = False):
+        """Enqueues source rays [ray_begin, ray_begin + n_rays); returns immediately."""
+        s = None if stream is None else C.c_void_p(int(stream))
+        self._check(self._L.rtg_trace_range(self._h, int(ray_begin), int(ray_begin + n_rays), int(seed),
+                                            1 if accumulate else 0, s))
+
+    def synchronize(self):
+        self._check(self._L.rtg_synchronize(self._h))
+
+    def request_abort(self):
+        self._check(self._L.rtg_request_abort(self._h))
+
+    def trace_rays(self, rays, tnear: float = 1e-4):
+        r = _f32(rays, (-1, 6))
+        prim = np.zeros(len(r), dtype=np.int32)
+        t = np.zeros(len(r), dtype=np.float32)
+        self._check(self._L.rtg_trace_rays(self._h, _ptr(r, L._f32p), len(r), float(tnear), _ptr(prim, L._i32p),
+                                           _ptr(t, L._f32p)))
+        return prim, t
+
+    # -- results --------------------------------------------------------------
+    def mc_estimates(self) -> np.ndarray:
+        out = np.zeros(self.num_primitives, dtype=np.float32)
+        self._check(self._L.rtg_get_mc_estimates(self._h, _ptr(out, L._f32p)))
+        return out
+
+    def hit_counts(self) -> np.ndarray:
+        out = np.zeros(self.num_primitives, dtype=np.uint64)
+        self._check(self._L.rtg_get_hit_counts(self._h, _ptr(out, L._u64p)))
+        return out
+
+    def accumulators(self):
+        n = self.num_primitives
+        s = [np.zeros(n) for _ in range(4)]
+        self._check(self._L.rtg_get_accumulators(self._h, *[_ptr(x, L._f64p) for x in s]))
+        return s
+
+    def values(self) -> np.ndarray:
+        return self.accumulators()[0]
+
+    def exposed_areas(self) -> np.ndarray:
+        out = np.zeros(self.num_primitives, dtype=np.float32)
+        self._check(self._L.rtg_get_exposed_areas(self._h, _ptr(out, L._f32p)))
+        return out
+
+    def relative_error(self) -> np.ndarray:
+        out = np.zeros(self.num_primitives)
+        self._check(self._L.rtg_get_relative_error(self._h, _ptr(out, L._f64p)))
+        return out
+
+    def vov(self) -> np.ndarray:
+        out = np.zeros(self.num_primitives)
+        self._check(self._L.rtg_get_vov(self._h, _ptr(out, L._f64p)))
+        return out
+
+    def tally(self) -> Tally:
+        t = L.RtgTally()
+        self._check(self._L.rtg_get_tally(self._h, C.byref(t)))
+        return Tally(t.num_rays, t.hitc, t.nonhitc, t.total, t.segments, t.truncated, t.nb_deposits, t.errors,
+                     t.trace_ms, t.kernel_ms)
+
+    def neighbors(self):
+        nnz = C.c_int64()
+        self._check(self._L.rtg_get_neighbors(self._h, None, None, 0, C.byref(nnz)))
+        rp = np.zeros(self.n_discs + 1, dtype=np.int64)
+        cols = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        self._check(self._L.rtg_get_neighbors(self._h, _ptr(rp, L._i64p), _ptr(cols, L._i32p), len(cols),
+                                              C.byref(nnz)))
+        return rp, cols[:nnz.value]
+
+    def device_view(self) -> L.RtgDeviceView:
+        v = L.RtgDeviceView()
+        self._check(self._L.rtg_get_device_view(self._h, C.byref(v)))
+        return v
+
+
+def device_run(points, normals, radii, *, n_rays: int, seed: int = 0, config: L.RtgConfig | None = None,
+               sticking_field=None, device: int = 0):
+    """rti::device::run in one C call: host arrays in, (estimates, hit counts) out."""
+    lib = L.load()
+    p, n, r = _f32(points, (-1, 3)), _f32(normals, (-1, 3)), _f32(radii, (-1,))
+    est = np.zeros(len(p), dtype=np.float32)
+    cnt = np.zeros(len(p), dtype=np.uint64)
+    sf = None if sticking_field is None else _f32(sticking_field, (-1,))
+    rc = lib.rtg_device_run(_ptr(p, L._f32p), _ptr(n, L._f32p), _ptr(r, L._f32p), len(p),
+                            None if config is None else C.byref(config),
+                            None if sf is None else _ptr(sf, L._f32p), int(n_rays), int(seed),
+                            _ptr(est, L._f32p), _ptr(cnt, L._u64p), int(device))
+    if rc != L.RTG_OK:
+        raise L.RtgError(rc, "rtg_device_run failed")
+    return est, cnt

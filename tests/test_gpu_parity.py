@@ -1,0 +1,254 @@
+"""GPU path (librtg through its C ABI) against the CPU oracle on the same inputs.
+
+Integer results (hit primitive ids, hit counts, tallies, neighbour lists) must
+match bit for bit; hit distances too.  FP64 accumulators differ only by the
+order of the additions: |S1_gpu - S1_cpu| <= 1e-9 * S1 (atomics on the GPU,
+per-thread sums on the CPU).  Areas use CUDA's acos/sin: rtol 2e-5.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from rti_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+S1_RTOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def eng(rtg_lib):
+    from rti_gb300 import Engine
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+@pytest.fixture(scope="module")
+def trench():
+    return scenes.trench_discs(domain=1.2, width=0.4, depth=1.0)
+
+
+@pytest.fixture(scope="module")
+def hole():
+    return scenes.hole_triangles(n_theta=128, n_wall=40, n_top=8, n_bottom=6, depth=4.0)
+
+
+def _random_rays(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    o = lo + (hi - lo) * rng.random((n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([o, d], 1).astype(np.float32)
+
+
+def _upload_discs(eng, t, **cfg):
+    eng.upload_discs(t.points, t.normals, t.radii)
+    eng.configure(box=(t.box_lo, t.box_hi), **cfg)
+
+
+def _compare_trace(g, c, np_):
+    cnt = g["counts"]
+    assert np.array_equal(cnt, c.counts), "hit counts differ"
+    assert g["tally"].hitc == c.hitc
+    assert g["tally"].nonhitc == c.nonhitc
+    assert g["tally"].total == c.total
+    assert g["tally"].segments == c.segments
+    assert g["tally"].truncated == c.truncated
+    assert g["tally"].nb_deposits == c.nb_deposits
+    assert g["tally"].errors == 0
+    for a, b in zip(g["s"], (c.s1, c.s2, c.s3, c.s4)):
+        np.testing.assert_allclose(a, b, rtol=S1_RTOL, atol=0)
+
+
+def _gpu_trace(eng, n, seed):
+    eng.trace(n, seed)
+    return {"counts": eng.hit_counts(), "s": eng.accumulators(), "tally": eng.tally()}
+
+
+def test_closest_hit_discs_bit_exact(eng, trench, oracle_lib):
+    _upload_discs(eng, trench)
+    lo = np.array(trench.box_lo, np.float32)
+    hi = np.array(trench.box_hi, np.float32)
+    rays = _random_rays(50000, lo, hi, 0)
+    pg, tg = eng.trace_rays(rays)
+    s = oracle_lib.Scene(trench.xyzr, trench.normals)
+    pc, tc = s.closest_hit(rays)
+    assert (pg >= 0).mean() > 0.5
+    assert np.array_equal(pg, pc)
+    assert np.array_equal(tg.view(np.uint32), tc.view(np.uint32))
+
+
+def test_closest_hit_triangles_bit_exact(eng, hole, oracle_lib):
+    eng.upload_triangles(hole.vertices, hole.indices)
+    rays = _random_rays(50000, np.array(hole.box_lo, np.float32), np.array(hole.box_hi, np.float32), 1)
+    pg, tg = eng.trace_rays(rays)
+    s = oracle_lib.Scene(tri_vertices=hole.vertices, tri_indices=hole.indices)
+    pc, tc = s.closest_hit(rays)
+    assert (pg >= 0).mean() > 0.5
+    assert np.array_equal(pg, pc)
+    assert np.array_equal(tg.view(np.uint32), tc.view(np.uint32))
+
+
+def test_compare_with_embree_two_discs(eng, oracle_lib):
+    """test/rti/trace/local_intersector.cpp:131-268 restated at this boundary:
+    two tilted discs, rays from z=10 to z=-1; whenever the closest hit is disc 1,
+    local_intersector must report a hit on disc 1 and none on disc 0."""
+    discs = np.array([[-2, -2, 0, 3], [3, 5, 0, 2.76]], np.float32)
+    nrm = np.array([[0.5, 0.2, 1], [0.1, -0.155, 1]], np.float64)
+    nrm = (nrm / np.linalg.norm(nrm, axis=1, keepdims=True)).astype(np.float32)
+    eng.upload_discs(discs[:, :3], nrm, discs[:, 3])
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    p1 = np.stack([rng.random(n) * 600 - 10, rng.random(n) * 20 - 10, np.full(n, 10.0)], 1)
+    p2 = np.stack([rng.random(n) * 20 - 10, rng.random(n) * 20 - 10, np.full(n, -1.0)], 1)
+    d = p2 - p1
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([p1, d], 1).astype(np.float32)
+    prim, _ = eng.trace_rays(rays, tnear=0.0)
+    idx = np.nonzero(prim == 1)[0]
+    assert len(idx) > 1000
+    for i in idx[:3000]:
+        o, dd = rays[i, :3], rays[i, 3:]
+        assert oracle_lib.local_intersect(o, dd, discs[1], nrm[1])
+        assert not oracle_lib.local_intersect(o, dd, discs[0], nrm[0])
+
+
+def test_neighbors_match_oracle(eng, trench, oracle_lib):
+    _upload_discs(eng, trench)
+    rg, cg = eng.neighbors()
+    s = oracle_lib.Scene(trench.xyzr, trench.normals)
+    rc, cc = s.neighbors()
+    assert np.array_equal(rg, rc) and np.array_equal(cg, cc)
+
+
+def test_neighbors_random_cloud(eng, oracle_lib):
+    rng = np.random.default_rng(7)
+    n = 20000
+    p = (rng.random((n, 3)) * [2.0, 2.0, 0.5]).astype(np.float32)
+    nrm = rng.normal(size=(n, 3))
+    nrm = (nrm / np.linalg.norm(nrm, axis=1, keepdims=True)).astype(np.float32)
+    r = (0.005 + 0.02 * rng.random(n)).astype(np.float32)
+    eng.upload_discs(p, nrm, r)
+    rg, cg = eng.neighbors()
+    s = oracle_lib.Scene(np.concatenate([p, r[:, None]], 1), nrm)
+    rc, cc = s.neighbors()
+    assert np.array_equal(rg, rc) and np.array_equal(cg, cc)
+
+
+@pytest.mark.parametrize("bound", [1, 0], ids=["periodic", "reflective"])
+def test_trace_trench_matches_oracle(eng, trench, oracle_lib, bound):
+    _upload_discs(eng, trench, sticking=0.1, x_bound=bound, y_bound=bound)
+    n = 200000
+    g = _gpu_trace(eng, n, seed=11)
+    s = oracle_lib.Scene(trench.xyzr, trench.normals)
+    s.neighbors()
+    cfg = oracle_lib.make_config(trench.box_lo, trench.box_hi, sticking=0.1, x_bound=bound, y_bound=bound, seed=11)
+    c = s.trace(cfg, 0, n)
+    assert c.hitc > n
+    _compare_trace(g, c, trench.n)
+
+
+def test_trace_hole_mixed_reflection_matches_oracle(eng, hole, oracle_lib):
+    eng.upload_triangles(hole.vertices, hole.indices)
+    eng.configure(box=(hole.box_lo, hole.box_hi), sticking=0.01, reflection=2, specular_fraction=0.1,
+                  x_bound=1, y_bound=1)
+    n = 100000
+    g = _gpu_trace(eng, n, seed=3)
+    s = oracle_lib.Scene(tri_vertices=hole.vertices, tri_indices=hole.indices)
+    cfg = oracle_lib.make_config(hole.box_lo, hole.box_hi, sticking=0.01, reflection=2, specular_fraction=0.1,
+                                 seed=3)
+    c = s.trace(cfg, 0, n)
+    assert c.hitc > 2 * n
+    _compare_trace(g, c, hole.n)
+
+
+def test_trace_power_cosine_and_sticking_field(eng, trench, oracle_lib):
+    rng = np.random.default_rng(9)
+    field = rng.uniform(0.05, 0.9, trench.n).astype(np.float32)
+    _upload_discs(eng, trench, source_exponent=5.0, reflection=1)
+    eng.set_sticking_field(field)
+    n = 100000
+    g = _gpu_trace(eng, n, seed=5)
+    eng.set_sticking_field(None)
+    s = oracle_lib.Scene(trench.xyzr, trench.normals)
+    s.neighbors()
+    cfg = oracle_lib.make_config(trench.box_lo, trench.box_hi, source_exponent=5.0, reflection=1, seed=5)
+    c = s.trace(cfg, 0, n, sticking_field=field)
+    _compare_trace(g, c, trench.n)
+
+
+def test_truncation_matches_oracle(eng, trench, oracle_lib):
+    _upload_discs(eng, trench, sticking=0.02, max_segments=3)
+    n = 50000
+    g = _gpu_trace(eng, n, seed=2)
+    s = oracle_lib.Scene(trench.xyzr, trench.normals)
+    s.neighbors()
+    cfg = oracle_lib.make_config(trench.box_lo, trench.box_hi, sticking=0.02, max_segments=3, seed=2)
+    c = s.trace(cfg, 0, n)
+    assert c.truncated > 0
+    _compare_trace(g, c, trench.n)
+    eng.configure(max_segments=1 << 16)
+
+
+def test_areas_estimates_and_stats(eng, trench, oracle_lib):
+    _upload_discs(eng, trench, sticking=0.1, x_bound=1, y_bound=1)
+    eng.trace(100000, 1)
+    ag = eng.exposed_areas()
+    s = oracle_lib.Scene(trench.xyzr, trench.normals)
+    rp, cols = s.neighbors()
+    ac = s.areas((trench.box_lo[0], trench.box_lo[1], trench.box_hi[0], trench.box_hi[1]))
+    np.testing.assert_allclose(ag, ac, rtol=2e-5, atol=1e-12)
+    s1, s2, s3, s4 = eng.accumulators()
+    cnt = eng.hit_counts()
+    tot = eng.tally().total
+    est = eng.mc_estimates()
+    ref = oracle_lib.normalize(s1, ag, rp, cols)
+    np.testing.assert_allclose(est, ref, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(eng.relative_error(), oracle_lib.relative_error(s1, s2, tot), rtol=1e-12)
+    np.testing.assert_allclose(eng.vov(), oracle_lib.vov(s1, s2, s3, s4, cnt, tot), rtol=1e-9)
+
+
+def test_area_known_answers_on_gpu(eng):
+    """The 37 exposed-area known answers, evaluated by the GPU area kernel."""
+    cases = json.load(open(os.path.join(GOLDEN, "area_inside_cases.json")))
+    by_box = {}
+    for c in cases:
+        by_box.setdefault(tuple(c["box"]), []).append(c)
+    for box, cs in by_box.items():
+        d = np.array([c["disc"] for c in cs], np.float32)
+        n = np.array([c["normal"] for c in cs], np.float64)
+        n = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+        eng.upload_discs(d[:, :3], n, d[:, 3])
+        eng.configure(box=((box[0], box[1], -100.0), (box[2], box[3], 100.0)))
+        a = eng.exposed_areas()
+        for c, v in zip(cs, a):
+            tol = max(c["tol"], 2e-6 * abs(c["expected"]))
+            assert abs(float(v) - c["expected"]) <= tol, (c["name"], float(v), c["expected"])
+
+
+def test_refit_after_move_equals_fresh_upload(eng, trench, oracle_lib):
+    _upload_discs(eng, trench, sticking=0.1, x_bound=1, y_bound=1)
+    moved = trench.points.copy()
+    moved[:, 2] += (0.003 * np.sin(moved[:, 0] * 7)).astype(np.float32)
+    eng.update_discs(moved, trench.normals, trench.radii)
+    eng.configure(box=(trench.box_lo, trench.box_hi))
+    a = _gpu_trace(eng, 50000, seed=4)
+    eng.upload_discs(moved, trench.normals, trench.radii)
+    eng.configure(box=(trench.box_lo, trench.box_hi))
+    b = _gpu_trace(eng, 50000, seed=4)
+    assert np.array_equal(a["counts"], b["counts"])
+    assert a["tally"].segments == b["tally"].segments
+
+
+def test_abort_returns_status(eng, trench):
+    from rti_gb300 import RtgError
+    _upload_discs(eng, trench, sticking=0.001, x_bound=1, y_bound=1)
+    eng.trace(50_000_000, 0)
+    eng.request_abort()
+    with pytest.raises(RtgError) as ei:
+        eng.hit_counts()
+    assert ei.value.code == 6
+    eng.configure(sticking=0.1)
