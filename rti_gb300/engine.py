@@ -115,10 +115,15 @@ class Engine:
     # -- configuration --------------------------------------------------------
     def configure(self, *, x_bound=None, y_bound=None, reflection=None, specular_fraction=None, sticking=None,
                   source_exponent=None, box=None, tnear=None, roulette_threshold=None, roulette_weight=None,
-                  max_segments=None, job=None):
-        """Updates the trace configuration; ``box`` = ((xlo, ylo, zlo), (xhi, yhi, zhi)) or None for rti's rule."""
+                  max_segments=None, job=None, reset=False):
+        """Updates the trace configuration (starting from rti's defaults when
+        ``reset``); ``box`` = ((xlo, ylo, zlo), (xhi, yhi, zhi)), else the box
+        stays as configured (rti's rule by default)."""
         c = L.RtgConfig()
-        self._check(self._L.rtg_get_config(self._h, C.byref(c)))
+        if reset:
+            self._L.rtg_config_default(C.byref(c))
+        else:
+            self._check(self._L.rtg_get_config(self._h, C.byref(c)))
         for name, val in (("x_bound", x_bound), ("y_bound", y_bound), ("reflection", reflection),
                           ("specular_fraction", specular_fraction), ("sticking", sticking),
                           ("source_exponent", source_exponent), ("tnear", tnear),

@@ -1,0 +1,65 @@
+"""Multi-rank path on CPU: two gloo ranks trace disjoint ray ranges with the
+oracle and sum their accumulators; the result equals one rank tracing every
+ray (counts and tallies bit for bit, S1..S4 to the FP64 summation order)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+from rti_gb300.sharding import allreduce_results, ray_range, stack_accumulators
+
+N_TOTAL = 6000
+
+
+def _scene():
+    from oracle import oracle as O
+    from rti_gb300 import scenes
+    t = scenes.trench_discs(domain=0.6, width=0.2, depth=0.4)
+    s = O.Scene(t.xyzr, t.normals)
+    s.neighbors()
+    cfg = O.make_config(t.box_lo, t.box_hi, sticking=0.2, seed=9)
+    return s, cfg
+
+
+def _worker(rank, world, port, out_dir):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    s, cfg = _scene()
+    b, e = ray_range(rank, world, N_TOTAL, scaling="strong")
+    r = s.trace(cfg, b, e, nthreads=1)
+    acc = torch.from_numpy(stack_accumulators(r.s1, r.s2, r.s3, r.s4))
+    cnt = torch.from_numpy(r.counts.astype(np.int64))
+    tally = {"hitc": r.hitc, "nonhitc": r.nonhitc, "total": r.total, "segments": r.segments}
+    allreduce_results(acc, cnt, tally)
+    if rank == 0:
+        np.save(os.path.join(out_dir, "acc.npy"), acc.numpy())
+        np.save(os.path.join(out_dir, "cnt.npy"), cnt.numpy())
+        np.save(os.path.join(out_dir, "tally.npy"), np.array([tally[k] for k in sorted(tally)]))
+    dist.destroy_process_group()
+
+
+def test_ray_range_partitions():
+    assert [ray_range(r, 3, 10, "strong") for r in range(3)] == [(0, 4), (4, 7), (7, 10)]
+    assert [ray_range(r, 2, 5, "weak") for r in range(2)] == [(0, 5), (5, 10)]
+    with pytest.raises(ValueError):
+        ray_range(2, 2, 5)
+
+
+def test_two_gloo_ranks_equal_one_rank(tmp_path, oracle_lib):
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    mp.start_processes(_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
+    s, cfg = _scene()
+    ref = s.trace(cfg, 0, N_TOTAL, nthreads=1)
+    acc = np.load(tmp_path / "acc.npy")
+    cnt = np.load(tmp_path / "cnt.npy")
+    tally = np.load(tmp_path / "tally.npy")
+    assert np.array_equal(cnt, ref.counts.astype(np.int64))
+    np.testing.assert_allclose(acc, stack_accumulators(ref.s1, ref.s2, ref.s3, ref.s4), rtol=1e-12)
+    assert list(tally) == [ref.hitc, ref.nonhitc, ref.segments, ref.total]
