@@ -202,7 +202,9 @@ def run_ours(args):
     eng.upload_triangles(h.vertices, h.indices)
     eng.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
                   x_bound=1, y_bound=1, source_exponent=1.0)
-    stream = torch.cuda.current_stream(dev)
+    # one dedicated stream for the flush, the events and librtg's kernels
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     view = eng.device_view()
     acc = None

@@ -159,8 +159,14 @@ class Engine:
 
     # -- tracing --------------------------------------------------------------
     def trace(self, n_rays: int, seed: int = 0, stream=None, *, ray_begin: int = 0, accumulate: bool = False):
-        """Enqueues source rays [ray_begin, ray_begin + n_rays); returns immediately."""
-        s = None if stream is None else C.c_void_p(int(stream))
+        """Enqueues source rays [ray_begin, ray_begin + n_rays); returns immediately.
+
+        stream: a cudaStream_t handle as an int (e.g. torch.cuda.Stream().cuda_stream);
+        0 is the legacy default stream (torch's default), None the context's own stream."""
+        if stream is None:
+            s = None
+        else:
+            s = C.c_void_p(int(stream) if int(stream) != 0 else 1)  # 1 == cudaStreamLegacy
         self._check(self._L.rtg_trace_range(self._h, int(ray_begin), int(ray_begin + n_rays), int(seed),
                                             1 if accumulate else 0, s))
 

@@ -168,7 +168,7 @@ def test_trace_hole_mixed_reflection_matches_oracle(eng, hole, oracle_lib):
 def test_trace_power_cosine_and_sticking_field(eng, trench, oracle_lib):
     rng = np.random.default_rng(9)
     field = rng.uniform(0.05, 0.9, trench.n).astype(np.float32)
-    _upload_discs(eng, trench, source_exponent=5.0, reflection=1)
+    _upload_discs(eng, trench, source_exponent=5.0, reflection=1, x_bound=1, y_bound=1)
     eng.set_sticking_field(field)
     n = 100000
     g = _gpu_trace(eng, n, seed=5)
@@ -181,7 +181,7 @@ def test_trace_power_cosine_and_sticking_field(eng, trench, oracle_lib):
 
 
 def test_truncation_matches_oracle(eng, trench, oracle_lib):
-    _upload_discs(eng, trench, sticking=0.02, max_segments=3)
+    _upload_discs(eng, trench, sticking=0.02, max_segments=3, x_bound=1, y_bound=1)
     n = 50000
     g = _gpu_trace(eng, n, seed=2)
     s = oracle_lib.Scene(trench.xyzr, trench.normals)
