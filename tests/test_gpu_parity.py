@@ -252,3 +252,24 @@ def test_abort_returns_status(eng, trench):
         eng.hit_counts()
     assert ei.value.code == 6
     eng.configure(sticking=0.1)
+
+
+def test_independent_streams_agree_within_4_sigma(eng, trench, oracle_lib):
+    """GPU (seed 100) and oracle (seed 200) are independent Monte Carlo runs:
+    the flux summed over 25 depth bands must agree within 4 sigma, sigma from
+    the S2 sums (x4 for the correlated neighbour deposits of one path)."""
+    _upload_discs(eng, trench, sticking=0.1, x_bound=1, y_bound=1)
+    n = 400000
+    g = _gpu_trace(eng, n, seed=100)
+    s = oracle_lib.Scene(trench.xyzr, trench.normals)
+    s.neighbors()
+    c = s.trace(oracle_lib.make_config(trench.box_lo, trench.box_hi, sticking=0.1, seed=200), 0, n)
+    z = trench.points[:, 2]
+    edges = np.quantile(z, np.linspace(0, 1, 26))
+    band = np.clip(np.searchsorted(edges, z, side="right") - 1, 0, 24)
+    xg = np.bincount(band, weights=g["s"][0], minlength=25)
+    xc = np.bincount(band, weights=c.s1, minlength=25)
+    var = 4 * (np.bincount(band, weights=g["s"][1], minlength=25) + np.bincount(band, weights=c.s2, minlength=25))
+    ok = xg + xc > 0
+    assert np.all(np.abs(xg - xc)[ok] <= 4 * np.sqrt(var[ok]))
+    assert not np.array_equal(g["counts"], c.counts)  # the streams really are independent
