@@ -167,6 +167,18 @@ RTG_API int rtg_get_tally(rtg_context* ctx, rtg_tally* out);
 /* Neighbour CSR of the discs: row_ptr (nd+1), cols (cap entries); *nnz gets the count. */
 RTG_API int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols, int64_t cap, int64_t* nnz);
 
+/* No counterpart in the reference.  The estimates of rtg_get_mc_estimates,
+ * written to a device buffer the caller owns (d_out, one float per primitive),
+ * enqueued on `stream` (NULL = the context's stream) after the trace and
+ * without allocating or freeing any device memory -- for callers whose GPU
+ * memory belongs to their own pool, or who cannot take the device-wide
+ * synchronisation that cudaFree implies.  Scratch is a fixed 256 KiB array in
+ * the library (at most 8388352 primitives; larger surfaces are rejected).
+ * The first call on a device looks that array up and should come before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race.
+ * The trace's status is not checked here (see rtg_get_tally). */
+RTG_API int rtg_get_mc_estimates_noalloc(rtg_context* ctx, float* d_out, void* stream);
+
 /* Device-resident views (valid until the geometry changes). */
 typedef struct rtg_device_view {
   double*   s1;        /* S1..S4 are consecutive arrays of n doubles */

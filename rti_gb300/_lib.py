@@ -36,7 +36,7 @@ EXPORTS = [
     "rtg_trace", "rtg_trace_range", "rtg_synchronize", "rtg_request_abort", "rtg_trace_rays",
     "rtg_num_primitives", "rtg_get_mc_estimates", "rtg_get_hit_counts", "rtg_get_accumulators",
     "rtg_get_exposed_areas", "rtg_get_relative_error", "rtg_get_vov", "rtg_get_tally",
-    "rtg_get_neighbors", "rtg_get_device_view", "rtg_device_run",
+    "rtg_get_neighbors", "rtg_get_device_view", "rtg_device_run", "rtg_get_mc_estimates_noalloc",
 ]
 
 
@@ -119,6 +119,7 @@ def load(path: str | None = None):
         "rtg_trace_rays": (C.c_int, [_ctx, _f32p, C.c_int64, C.c_float, _i32p, _f32p]),
         "rtg_num_primitives": (C.c_int, [_ctx, _i64p]),
         "rtg_get_mc_estimates": (C.c_int, [_ctx, _f32p]),
+        "rtg_get_mc_estimates_noalloc": (C.c_int, [_ctx, C.c_void_p, C.c_void_p]),
         "rtg_get_hit_counts": (C.c_int, [_ctx, _u64p]),
         "rtg_get_accumulators": (C.c_int, [_ctx, _f64p, _f64p, _f64p, _f64p]),
         "rtg_get_exposed_areas": (C.c_int, [_ctx, _f32p]),

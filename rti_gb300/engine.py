@@ -190,6 +190,13 @@ class Engine:
         self._check(self._L.rtg_get_mc_estimates(self._h, _ptr(out, L._f32p)))
         return out
 
+    def mc_estimates_noalloc(self, d_out: int, stream=None):
+        """Writes the normalised estimates into the caller's device buffer at
+        address d_out (float32 per primitive) without allocating device memory;
+        enqueued on `stream` (int handle) or the context's stream."""
+        s = None if stream is None else C.c_void_p(int(stream) if int(stream) != 0 else 1)
+        self._check(self._L.rtg_get_mc_estimates_noalloc(self._h, C.c_void_p(int(d_out)), s))
+
     def hit_counts(self) -> np.ndarray:
         out = np.zeros(self.num_primitives, dtype=np.uint64)
         self._check(self._L.rtg_get_hit_counts(self._h, _ptr(out, L._u64p)))
