@@ -293,6 +293,30 @@ def run_ours(args):
                "d2h_bytes_per_step": int(16 * np_),
                "includes": "context creation, upload, LBVH build, trace, hit counts + S1 read back"}
 
+    # adjoint replay (d/d sticking and d/d exponent of the bottom-quarter flux)
+    adj = None
+    if not args.no_adjoint:
+        V = h.vertices.astype(np.float64)
+        zc = V[h.indices].mean(axis=1)[:, 2]
+        g = torch.from_numpy((zc < -0.75 * h.meta["depth"]).astype(np.float64)).to(dev)
+        sc = torch.zeros(2, dtype=torch.float64, device=dev)
+        t_adj = []
+        for k in range(args.warmup + 3):
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            a0.record(stream)
+            eng.adjoint_device(g.data_ptr(), rank * R, (rank + 1) * R, k, 0, sc.data_ptr(), unbiased=True,
+                               stream=stream.cuda_stream)
+            a1.record(stream)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                t_adj.append(a0.elapsed_time(a1))
+        fwd_ms = statistics.mean(step_ms)
+        adj_ms = statistics.mean(t_adj)
+        adj = {"workload": "bottom-quarter flux of the same hole, d/d sticking (unbiased) and d/d exponent",
+               "adjoint_ms": adj_ms, "forward_ms": fwd_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+               "grad_evals_per_s": 1e3 / (fwd_ms + adj_ms), "rays_per_grad_eval": R}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rays_s, _ = cpu_sample(h, args.cpu_rays, os.cpu_count() or 1)
@@ -303,7 +327,7 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f64 accumulators",
                 "data": "synthetic", "config": config_dict(h, R), "clocks": clocks, "roofline": roof,
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps, "adjoint": adj,
                 "wall_s_timed_region": wall,
                 "tally_per_step": {"segments": seg, "hitc": statistics.mean(t.hitc for t in tallies),
                                    "truncated": max(t.truncated for t in tallies),
@@ -326,6 +350,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     from __graft_entry__ import build

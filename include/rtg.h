@@ -150,6 +150,28 @@ RTG_API int rtg_synchronize(rtg_context* ctx);
 /* Asks a running trace to stop; it returns RTG_ERR_ABORTED. */
 RTG_API int rtg_request_abort(rtg_context* ctx);
 
+/* Per-primitive sticking from a device array (e.g. a torch tensor); NULL clears it. */
+RTG_API int rtg_set_sticking_field_device(rtg_context* ctx, const float* d_field, int64_t n, void* stream);
+
+/* Adjoint of the trace (no counterpart in rti; the differentiation path).
+ * With L = sum_i g_i * S1_i, replays source rays [ray_begin, ray_end) of the
+ * trace with `seed` under the current surface and configuration and ADDS
+ *   d_scalars[0] += dL/ds  (global sticking; 0 when a sticking field is set),
+ *   d_scalars[1] += dL/dn  (source cosine exponent, score-function estimator),
+ *   d_field_grad[j] += dL/ds_j (when a sticking field is set; required then).
+ * estimator: RTG_ADJ_HELD holds the Russian-roulette decisions as drawn (what
+ * central differences with common random numbers measure); RTG_ADJ_UNBIASED
+ * adds the likelihood ratio of each roulette survival (an unbiased gradient of
+ * the expected flux).  All pointers are device pointers; enqueued on `stream`.
+ * Same paths as the forward trace (same Philox counters); no per-path memory. */
+#define RTG_ADJ_HELD 0
+#define RTG_ADJ_UNBIASED 1
+RTG_API int rtg_adjoint(rtg_context* ctx, const double* d_g, uint64_t ray_begin, uint64_t ray_end, uint64_t seed,
+                        int estimator, double* d_field_grad, double* d_scalars, void* stream);
+/* Host-array form of rtg_adjoint for rays [0, n_rays); synchronous. */
+RTG_API int rtg_adjoint_host(rtg_context* ctx, const double* g, uint64_t n_rays, uint64_t seed, int estimator,
+                             double* field_grad, double* d_sticking, double* d_exponent);
+
 /* Closest hit for explicit rays: rays = n x 6 floats (origin, direction),
  * host pointers.  prim_out = primitive id or -1, t_out = distance. */
 RTG_API int rtg_trace_rays(rtg_context* ctx, const float* rays, int64_t n, float tnear, int32_t* prim_out,

@@ -85,6 +85,9 @@ def lib():
         L.orc_trace.restype = C.c_int
         L.orc_trace.argtypes = [C.c_void_p, C.POINTER(OrcConfig), C.c_uint64, C.c_uint64, C.c_int,
                                 _f64p, _f64p, _f64p, _f64p, _u64p, C.POINTER(OrcTally)]
+        L.orc_adjoint.restype = C.c_int
+        L.orc_adjoint.argtypes = [C.c_void_p, C.POINTER(OrcConfig), C.c_uint64, C.c_uint64, C.c_int, _f64p, C.c_int,
+                                  _f64p, _f64p, _u64p]
         L.orc_source_ray.argtypes = [C.POINTER(OrcConfig), C.c_uint64, _f32p, _f32p]
         L.orc_diffuse_dir.argtypes = [_f32p, C.c_uint32, C.c_uint32, _f32p]
         L.orc_philox4x32_10.argtypes = [_u32p, _u32p, _u32p]
@@ -223,6 +226,29 @@ class Scene:
         del keep
         return TraceResult(s1[:n], s2[:n], s3[:n], s4[:n], cnt[:n], tally.hitc, tally.nonhitc, tally.total,
                            tally.segments, tally.truncated, tally.nb_deposits)
+
+
+def adjoint(scene: "Scene", cfg: OrcConfig, g, ray_begin: int, ray_end: int, nthreads: int = 0,
+            sticking_field=None, unbiased: bool = False):
+    """Oracle adjoint replay: returns (dL/ds, dL/dn, dL/ds_j or None, segments)."""
+    gg = np.ascontiguousarray(g, dtype=np.float64)
+    keep = None
+    fg = None
+    if sticking_field is not None:
+        keep = np.ascontiguousarray(sticking_field, dtype=np.float32)
+        cfg.sticking_field = _p(keep, _f32p)
+        fg = np.zeros(scene.np)
+    else:
+        cfg.sticking_field = None
+    sc = np.zeros(2)
+    segs = C.c_uint64()
+    rc = lib().orc_adjoint(scene._h, C.byref(cfg), ray_begin, ray_end, nthreads, _p(gg, _f64p), int(unbiased),
+                           None if fg is None else _p(fg, _f64p), _p(sc, _f64p), C.byref(segs))
+    cfg.sticking_field = None
+    del keep
+    if rc != 0:
+        raise RuntimeError("orc_adjoint failed")
+    return sc[0], sc[1], fg, segs.value
 
 
 def make_config(box_lo, box_hi, *, x_bound=1, y_bound=1, reflection=0, specular_fraction=0.0,

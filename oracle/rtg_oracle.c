@@ -712,6 +712,189 @@ static void trace_path(const orc_scene* s, const orc_config* cf, uint64_t id, ac
   }
 }
 
+/* Adjoint replay of one path: derivatives of L = sum_i g_i S1_i.  G_k is the
+ * sum of g over the primitives that received deposit k, v_k = w_k s its
+ * weight (s the sticking of the hit primitive), P_k = sum_{m<=k} G_m v_m.
+ * Two estimators (cf->adj_unbiased):
+ *  held (0): the Russian-roulette decisions are held as drawn, which is what
+ *    central differences with common random numbers measure.  Within a
+ *    stretch between roulette resets every weight carries the factors (1 - s_e)
+ *    of the earlier deposits of the stretch, so
+ *      dL/ds_j = sum over deposits k on j of G_k w_k - (T - P_k)/(1 - s_j),
+ *    T the stretch total; one global s: v_k = w_k s, dv_k/ds = w_k + s w'_k,
+ *    w'_{k+1} = w'_k - dv_k/ds, w' = 0 after a reset.
+ *  unbiased (1): adds the likelihood ratio of each roulette survival
+ *    (probability w/0.3), which extends T to the whole path total L_p:
+ *      dL/ds_j = sum over deposits k on j of G_k w_k - (L_p - P_k)/(1 - s_j).
+ * A sticking field replays each stretch (held) or the whole path (unbiased)
+ * twice from a snapshot of its start: first for T, then to scatter.  Both:
+ *   dL/dn = sum over paths of (1/(n+1) + ln cos theta_0) L_p. */
+typedef struct { double ds, dn; double* field; } adj_acc_t;
+
+static void adjoint_path(const orc_scene* s, const orc_config* cf, uint64_t id, const double* g, int unbiased,
+                         adj_acc_t* a, uint64_t* segs) {
+  const int fieldmode = cf->sticking_field != NULL;
+  float org[3], dir[3];
+  orc_source_ray(cf, id, org, dir);
+  v3 o = mk(org[0], org[1], org[2]), d = mk(dir[0], dir[1], dir[2]);
+  float w = 1.0f;
+  uint32_t k = 0, nseg = 0;
+  const double score = 1.0 / ((double)cf->source_exponent + 1.0) + log(-(double)d.z);
+  double wd = 0.0, lp = 0.0, seg_t = 0.0, seg_p = 0.0, pa = 0.0, psum = 0.0, ncoll = 0.0;
+  int sub = 0;
+  v3 so = o, sd = d;
+  float sw = w;
+  uint32_t sk = k, snseg = nseg;
+  const double lower = cf->roulette_threshold * 1.0f, renew = cf->roulette_weight * 1.0f;
+  const float s_glob = cf->sticking;
+  for (;;) {
+    int ended = 0;
+    if (nseg == cf->max_segments) {
+      ended = 1;
+    } else {
+      nseg += 1;
+      *segs += 1;
+      float th = 0.0f, tb = 0.0f;
+      int32_t p = -1;
+      int hit = closest(s, o, d, cf->tnear, &th, &p);
+      int axis = boundary_exit(cf, o, d, &tb);
+      if (hit && (axis < 0 || th <= tb)) {
+        v3 n = prim_normal(s, p);
+        v3 hp = mk(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
+        if (d.x * n.x + d.y * n.y + d.z * n.z > 0.0f) {
+          o = hp;
+          continue;
+        }
+        float st = cf->sticking_field ? cf->sticking_field[p] : s_glob;
+        float v = w * st;
+        double G = g[p];
+        if (p < s->nd && s->nb_ptr)
+          for (int64_t q = s->nb_ptr[p]; q < s->nb_ptr[p + 1]; ++q) {
+            int32_t nb = s->nb_idx[q];
+            if (local_intersect(o, d, disc_c(s, nb), s->dc[4 * nb + 3], disc_n(s, nb))) G += g[nb];
+          }
+        const double gv = G * (double)v;
+        if (!fieldmode) {
+          lp += gv;
+          if (unbiased) {
+            pa += G * (double)w;
+            psum += lp;
+            ncoll += 1.0;
+          } else {
+            double dv = (double)w + (double)st * wd;
+            a->ds += G * dv;
+            wd -= dv;
+          }
+        } else if (sub == 0) {
+          seg_t += gv;
+        } else {
+          seg_p += gv;
+          lp += gv;
+          double gr = G * (double)w;
+          if (st < 1.0f) gr -= (seg_t - seg_p) / (1.0 - (double)st);
+          a->field[p] += gr;
+        }
+        w = w - v;
+        if (w == 0.0f) {
+          ended = 1;
+        } else {
+          uint32_t u[4];
+          draw4(cf->seed, id, k, cf->job, u);
+          int reset = 0;
+          if (!((double)w >= lower)) {
+            double kill = 1.0f - (double)w / renew;
+            if ((double)u[0] < kill * 4294967296.0) ended = 1;
+            else {
+              w = (float)renew;
+              reset = 1;
+              wd = 0.0;
+            }
+          }
+          if (!ended) {
+            int spec = cf->reflection == 1 ||
+                       (cf->reflection == 2 && (double)u[3] < (double)cf->specular_fraction * 4294967296.0);
+            d = spec ? specular_dir(n, d) : diffuse_dir(n, u[1], u[2]);
+            o = hp;
+            k += 1;
+            if (fieldmode && reset && !unbiased) {
+              if (sub == 0) {
+                o = so; d = sd; w = sw; k = sk; nseg = snseg;
+                seg_p = 0.0; sub = 1;
+              } else {
+                so = o; sd = d; sw = w; sk = k; snseg = nseg;
+                seg_t = 0.0; seg_p = 0.0; sub = 0;
+              }
+            }
+            continue;
+          }
+        }
+      } else if (axis >= 0) {
+        v3 hp = mk(o.x + d.x * tb, o.y + d.y * tb, o.z + d.z * tb);
+        int periodic = axis == 0 ? cf->x_bound : cf->y_bound;
+        if (periodic) {
+          if (axis == 0) hp.x = d.x > 0.0f ? cf->box_lo[0] : cf->box_hi[0];
+          else hp.y = d.y > 0.0f ? cf->box_lo[1] : cf->box_hi[1];
+        } else {
+          if (axis == 0) d.x = -d.x;
+          else d.y = -d.y;
+        }
+        o = hp;
+        continue;
+      } else {
+        ended = 1;
+      }
+    }
+    if (ended) {
+      if (fieldmode && sub == 0) {
+        o = so; d = sd; w = sw; k = sk; nseg = snseg;
+        seg_p = 0.0; sub = 1;
+        continue;
+      }
+      if (!fieldmode && unbiased) {
+        double ds = pa;
+        if (s_glob < 1.0f) ds -= (ncoll * lp - psum) / (1.0 - (double)s_glob);
+        a->ds += ds;
+      }
+      a->dn += score * lp;
+      return;
+    }
+  }
+}
+
+int orc_adjoint(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, int nthreads, const double* g,
+                int unbiased, double* field_grad, double* scalars, uint64_t* segments) {
+  int64_t np = s->np;
+  if (cf->sticking_field && !field_grad) return 1;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  double ds = 0.0, dn = 0.0;
+  uint64_t segs = 0;
+#pragma omp parallel num_threads(nthreads)
+  {
+    adj_acc_t a = {0.0, 0.0, NULL};
+    uint64_t sg = 0;
+    if (cf->sticking_field) a.field = (double*)calloc((size_t)np + 1, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = (int64_t)b; i < (int64_t)e; ++i) adjoint_path(s, cf, (uint64_t)i, g, unbiased, &a, &sg);
+#pragma omp critical
+    {
+      ds += a.ds;
+      dn += a.dn;
+      segs += sg;
+      if (a.field)
+        for (int64_t p = 0; p < np; ++p) field_grad[p] += a.field[p];
+    }
+    free(a.field);
+  }
+  scalars[0] += ds;
+  scalars[1] += dn;
+  if (segments) *segments = segs;
+  return 0;
+}
+
 int orc_trace(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, int nthreads,
               double* s1, double* s2, double* s3, double* s4, uint64_t* cnt, orc_tally* tally) {
   int64_t np = s->np;

@@ -84,6 +84,13 @@ int orc_trace(const orc_scene* s, const orc_config* cf, uint64_t ray_begin, uint
               int nthreads, double* s1, double* s2, double* s3, double* s4, uint64_t* cnt,
               orc_tally* tally);
 
+/* Adjoint replay of rays [ray_begin, ray_end): with L = sum_i g_i S1_i adds
+ * dL/ds (global sticking) to scalars[0] and dL/dn (source exponent) to
+ * scalars[1]; with a sticking field in cf adds dL/ds_j to field_grad.
+ * unbiased = 0 holds the roulette decisions as drawn, 1 adds their likelihood ratio. */
+int orc_adjoint(const orc_scene* s, const orc_config* cf, uint64_t ray_begin, uint64_t ray_end, int nthreads,
+                const double* g, int unbiased, double* field_grad, double* scalars, uint64_t* segments);
+
 /* One source ray (origin, direction) for ray id; exposes the sampler. */
 void orc_source_ray(const orc_config* cf, uint64_t id, float* org, float* dir);
 /* Diffuse re-emission direction about a normal for two uniforms. */

@@ -37,7 +37,11 @@ EXPORTS = [
     "rtg_num_primitives", "rtg_get_mc_estimates", "rtg_get_hit_counts", "rtg_get_accumulators",
     "rtg_get_exposed_areas", "rtg_get_relative_error", "rtg_get_vov", "rtg_get_tally",
     "rtg_get_neighbors", "rtg_get_device_view", "rtg_device_run", "rtg_get_mc_estimates_noalloc",
+    "rtg_set_sticking_field_device", "rtg_adjoint", "rtg_adjoint_host",
 ]
+
+RTG_ADJ_HELD = 0
+RTG_ADJ_UNBIASED = 1
 
 
 class RtgConfig(C.Structure):
@@ -112,6 +116,10 @@ def load(path: str | None = None):
         "rtg_get_box": (C.c_int, [_ctx, _f32p, _f32p]),
         "rtg_set_sticking": (C.c_int, [_ctx, C.c_float]),
         "rtg_set_sticking_field": (C.c_int, [_ctx, _f32p, C.c_int64]),
+        "rtg_set_sticking_field_device": (C.c_int, [_ctx, C.c_void_p, C.c_int64, C.c_void_p]),
+        "rtg_adjoint": (C.c_int, [_ctx, C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p,
+                                  C.c_void_p, C.c_void_p]),
+        "rtg_adjoint_host": (C.c_int, [_ctx, _f64p, C.c_uint64, C.c_uint64, C.c_int, _f64p, _f64p, _f64p]),
         "rtg_trace": (C.c_int, [_ctx, C.c_uint64, C.c_uint64, C.c_void_p]),
         "rtg_trace_range": (C.c_int, [_ctx, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]),
         "rtg_synchronize": (C.c_int, [_ctx]),

@@ -172,6 +172,54 @@ int upload_triangles_impl(rtg_context* ctx, const float* vertices, const uint32_
   return RTG_OK;
 }
 
+// Checks the context and fills the kernel parameters of a trace (or of its
+// adjoint replay) of source rays [ray_begin, ray_end).
+int prepare_trace(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, TraceParams& p) {
+  if (ray_end < ray_begin) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "ray_end < ray_begin");
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  if (np == 0 || !ctx->g.nodes.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no geometry uploaded");
+  RTG_TRY(use_device(ctx));
+  const rtg_config& c = ctx->cfg;
+  for (int a = 0; a < 2; ++a)
+    if (!(ctx->box_lo[a] < ctx->box_hi[a]))
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "degenerate x/y box (all discs on one line?)");
+  *ctx->h_abort = 0;
+  p = TraceParams{};
+  p.s = scene_view(ctx);
+  p.s1 = ctx->acc.p;
+  p.s2 = ctx->acc.p + np;
+  p.s3 = ctx->acc.p + 2 * np;
+  p.s4 = ctx->acc.p + 3 * np;
+  p.cnt = ctx->cnt.p;
+  p.tally = ctx->d_tally;
+  p.abort_flag = ctx->d_abort;
+  p.ray_begin = ray_begin;
+  p.ray_end = ray_end;
+  p.seed = seed;
+  for (int a = 0; a < 3; ++a) {
+    p.box_lo[a] = ctx->box_lo[a];
+    p.box_hi[a] = ctx->box_hi[a];
+  }
+  p.src_lo[0] = ctx->box_lo[0];
+  p.src_lo[1] = ctx->box_lo[1];
+  p.src_hi[0] = ctx->box_hi[0];
+  p.src_hi[1] = ctx->box_hi[1];
+  p.tnear = c.tnear;
+  p.sticking = c.sticking;
+  p.source_exponent = c.source_exponent;
+  p.source_ee = 2.0f / (c.source_exponent + 1.0f);
+  p.specular_fraction = c.specular_fraction;
+  p.roulette_threshold = c.roulette_threshold;
+  p.roulette_weight = c.roulette_weight;
+  p.x_periodic = c.x_bound == RTG_BOUND_PERIODIC;
+  p.y_periodic = c.y_bound == RTG_BOUND_PERIODIC;
+  p.reflection = c.reflection;
+  p.max_segments = c.max_segments;
+  p.job = c.job;
+  p.adj_inv_n1 = 1.0 / ((double)c.source_exponent + 1.0);
+  return RTG_OK;
+}
+
 int rebuild_all(rtg_context* ctx) {
   RTG_TRY(build_lbvh(ctx));
   RTG_TRY(build_neighbors(ctx));
@@ -223,6 +271,10 @@ int rtg_create(rtg_context** out, int device) {
     if ((rc = use_device(ctx)) != RTG_OK) break;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = RTG_ERR_CUDA; break; }
     if (cudaMalloc((void**)&ctx->d_tally, sizeof(DevTally)) != cudaSuccess) { rc = RTG_ERR_OUT_OF_MEMORY; break; }
+    if (cudaMalloc((void**)&ctx->d_tally_adj, sizeof(DevTally)) != cudaSuccess) {
+      rc = RTG_ERR_OUT_OF_MEMORY;
+      break;
+    }
     if (cudaHostAlloc((void**)&ctx->h_abort, sizeof(uint32_t), cudaHostAllocMapped) != cudaSuccess) {
       rc = RTG_ERR_CUDA;
       break;
@@ -257,6 +309,7 @@ int rtg_destroy(rtg_context* ctx) {
   dfree(ctx->sticking_field); dfree(ctx->acc); dfree(ctx->cnt); dfree(ctx->areas); dfree(ctx->est);
   dfree(ctx->stat_tmp);
   if (ctx->d_tally) cudaFree(ctx->d_tally);
+  if (ctx->d_tally_adj) cudaFree(ctx->d_tally_adj);
   if (ctx->h_abort) cudaFreeHost(ctx->h_abort);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -396,48 +449,10 @@ int rtg_set_sticking_field(rtg_context* ctx, const float* s, int64_t n) {
 int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, int accumulate,
                     void* stream) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
-  if (ray_end < ray_begin) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "ray_end < ray_begin");
-  const int64_t np = ctx->g.nd + ctx->g.nt;
-  if (np == 0 || !ctx->g.nodes.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no geometry uploaded");
-  RTG_TRY(use_device(ctx));
-  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  const rtg_config& c = ctx->cfg;
-  for (int a = 0; a < 3; ++a)
-    if (!(ctx->box_lo[a] < ctx->box_hi[a]) && a < 2)
-      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "degenerate x/y box (all discs on one line?)");
-  *ctx->h_abort = 0;
   TraceParams p{};
-  p.s = scene_view(ctx);
-  p.s1 = ctx->acc.p;
-  p.s2 = ctx->acc.p + np;
-  p.s3 = ctx->acc.p + 2 * np;
-  p.s4 = ctx->acc.p + 3 * np;
-  p.cnt = ctx->cnt.p;
-  p.tally = ctx->d_tally;
-  p.abort_flag = ctx->d_abort;
-  p.ray_begin = ray_begin;
-  p.ray_end = ray_end;
-  p.seed = seed;
-  for (int a = 0; a < 3; ++a) {
-    p.box_lo[a] = ctx->box_lo[a];
-    p.box_hi[a] = ctx->box_hi[a];
-  }
-  p.src_lo[0] = ctx->box_lo[0];
-  p.src_lo[1] = ctx->box_lo[1];
-  p.src_hi[0] = ctx->box_hi[0];
-  p.src_hi[1] = ctx->box_hi[1];
-  p.tnear = c.tnear;
-  p.sticking = c.sticking;
-  p.source_exponent = c.source_exponent;
-  p.source_ee = 2.0f / (c.source_exponent + 1.0f);
-  p.specular_fraction = c.specular_fraction;
-  p.roulette_threshold = c.roulette_threshold;
-  p.roulette_weight = c.roulette_weight;
-  p.x_periodic = c.x_bound == RTG_BOUND_PERIODIC;
-  p.y_periodic = c.y_bound == RTG_BOUND_PERIODIC;
-  p.reflection = c.reflection;
-  p.max_segments = c.max_segments;
-  p.job = c.job;
+  RTG_TRY(prepare_trace(ctx, ray_begin, ray_end, seed, p));
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   RTG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   if (!accumulate) {
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * np * sizeof(double), st));
@@ -456,6 +471,86 @@ int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint
   ctx->traced = true;
   ctx->finalized = false;
   return RTG_OK;
+}
+
+int rtg_set_sticking_field_device(rtg_context* ctx, const float* d_field, int64_t n, void* stream) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  if (!d_field) {
+    dfree(ctx->sticking_field);
+    return RTG_OK;
+  }
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  if (n != np) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "sticking field length != number of primitives");
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  RTG_TRY(dalloc(ctx, ctx->sticking_field, (size_t)n, "sticking field"));
+  RTG_CUDA(ctx, cudaMemcpyAsync(ctx->sticking_field.p, d_field, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  return RTG_OK;
+}
+
+int rtg_adjoint(rtg_context* ctx, const double* d_g, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, int estimator,
+                double* d_field_grad, double* d_scalars, void* stream) {
+  if (!ctx || !d_g || !d_scalars) return RTG_ERR_INVALID_ARGUMENT;
+  const bool field = ctx->sticking_field.p != nullptr;
+  if (field && !d_field_grad)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a sticking field is set: d_field_grad is required");
+  TraceParams p{};
+  RTG_TRY(prepare_trace(ctx, ray_begin, ray_end, seed, p));
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  p.tally = ctx->d_tally_adj;
+  p.s1 = p.s2 = p.s3 = p.s4 = nullptr;
+  p.cnt = nullptr;
+  p.adj_g = d_g;
+  p.adj_field = field ? d_field_grad : nullptr;
+  p.adj_scalars = d_scalars;
+  p.adj_unbiased = estimator == RTG_ADJ_UNBIASED ? 1 : 0;
+  RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally_adj, 0, sizeof(DevTally), st));
+  if (ray_end > ray_begin) RTG_TRY(launch_trace(ctx, p, st, field ? kModeAdjField : kModeAdjGlobal));
+  return RTG_OK;
+}
+
+int rtg_adjoint_host(rtg_context* ctx, const double* g, uint64_t n_rays, uint64_t seed, int estimator, double* field_grad,
+                     double* d_sticking, double* d_exponent) {
+  if (!ctx || !g) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  const bool field = ctx->sticking_field.p != nullptr;
+  if (field && !field_grad)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a sticking field is set: field_grad is required");
+  DBuf<double> dg, df, ds;
+  int rc = dalloc(ctx, dg, (size_t)(np > 0 ? np : 1), "adjoint weights");
+  if (rc == RTG_OK) rc = dalloc(ctx, df, (size_t)(field ? np : 1), "adjoint field");
+  if (rc == RTG_OK) rc = dalloc(ctx, ds, 2, "adjoint scalars");
+  cudaStream_t st = ctx->stream;
+  if (rc == RTG_OK) {
+    cudaError_t e = cudaMemcpyAsync(dg.p, g, np * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(df.p, 0, df.n * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ds.p, 0, 2 * sizeof(double), st);
+    if (e != cudaSuccess) rc = check_cuda(ctx, e, "adjoint upload");
+  }
+  if (rc == RTG_OK) rc = rtg_adjoint(ctx, dg.p, 0, n_rays, seed, estimator, field ? df.p : nullptr, ds.p, nullptr);
+  double sc[2] = {0.0, 0.0};
+  if (rc == RTG_OK) {
+    cudaError_t e = cudaMemcpyAsync(sc, ds.p, sizeof sc, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && field) e = cudaMemcpyAsync(field_grad, df.p, np * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = check_cuda(ctx, e, "adjoint");
+  }
+  if (rc == RTG_OK) {
+    DevTally t;
+    if (cudaMemcpy(&t, ctx->d_tally_adj, sizeof t, cudaMemcpyDeviceToHost) == cudaSuccess) {
+      if (t.abort_seen) rc = set_error(ctx, RTG_ERR_ABORTED, "adjoint aborted on request");
+      else if (t.errors) rc = set_error(ctx, RTG_ERR_BUDGET, "a device-side traversal limit was reached");
+    }
+  }
+  dfree(dg);
+  dfree(df);
+  dfree(ds);
+  if (rc == RTG_OK) {
+    if (d_sticking) *d_sticking = sc[0];
+    if (d_exponent) *d_exponent = sc[1];
+  }
+  return rc;
 }
 
 int rtg_trace(rtg_context* ctx, uint64_t n_rays, uint64_t seed, void* stream) {

@@ -5,7 +5,7 @@
 #include <cstdint>
 #include <string>
 
-#include "../../include/rtg.h"
+#include "rtg.h"
 
 namespace rtg {
 
@@ -76,7 +76,19 @@ struct TraceParams {
   int32_t reflection;
   uint32_t max_segments;
   uint32_t job;
+  // adjoint replay (unused by the forward trace)
+  const double* adj_g;     // dL/dS1 by primitive id
+  double* adj_field;       // dL/ds_j by primitive id (sticking-field mode) or nullptr
+  double* adj_scalars;     // [0] dL/ds (global sticking), [1] dL/dn (source exponent)
+  double adj_inv_n1;       // 1 / (n + 1)
+  int32_t adj_unbiased;    // 0: roulette decisions held as drawn; 1: with their likelihood ratio
 };
+
+// Path-kernel modes: the forward trace, and two adjoint replays of the same
+// paths (same Philox counters, same arithmetic).
+constexpr int kModeForward = 0;
+constexpr int kModeAdjGlobal = 1;  // dL/ds (one global sticking) and dL/dn
+constexpr int kModeAdjField = 2;   // dL/ds_j (sticking field) and dL/dn
 
 // ---- device buffers owned by a context ----
 template <typename T>
@@ -125,6 +137,7 @@ struct rtg_context {
   rtg::DBuf<float> est;
   rtg::DBuf<double> stat_tmp;
   rtg::DevTally* d_tally = nullptr;
+  rtg::DevTally* d_tally_adj = nullptr;  // counters of adjoint replays
   uint32_t* h_abort = nullptr;  // host-mapped flag
   uint32_t* d_abort = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
@@ -151,7 +164,7 @@ int compute_areas(rtg_context* ctx, cudaStream_t st, const float* box_lo, const 
 int finalize_estimates(rtg_context* ctx, cudaStream_t st);
 int compute_stats(rtg_context* ctx, cudaStream_t st, uint64_t total, double* d_rel, double* d_vov);
 // trace.cu
-int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st);
+int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st, int mode = kModeForward);
 int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim,
                        float* d_t, cudaStream_t st);
 SceneView scene_view(rtg_context* ctx);

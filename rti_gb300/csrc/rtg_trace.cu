@@ -162,7 +162,32 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
   return v;
 }
 
-__global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceParams p) {
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+  return v;
+}
+
+// kModeForward traces and deposits.  The adjoint modes replay the same paths
+// and accumulate derivatives of L = sum_i g_i S1_i instead.  G_k = the sum of g
+// over the primitives that received deposit k, v_k = w_k s its weight,
+// P_k = sum_{m<=k} G_m v_m.
+//   held (adj_unbiased = 0): the roulette decisions are held as drawn (what
+//     central differences with common random numbers measure).  Within a
+//     stretch between roulette resets the weight is a product of (1 - s_e)
+//     factors, so dL/ds_j = sum over deposits k on j of G_k w_k - (T - P_k) /
+//     (1 - s_j), T the stretch total.  One global s: dv_k/ds = w_k + s w'_k,
+//     w'_{k+1} = w'_k - dv_k/ds, w' = 0 after a reset.
+//   unbiased (adj_unbiased = 1): adds the likelihood ratio of each roulette
+//     survival (probability w/0.3); T becomes the path total L_p.  One global
+//     s: dL/ds = sum_k G_k w_k - (K L_p - sum_k P_k)/(1 - s) over K deposits.
+//   kModeAdjField traces each stretch (held) or the whole path (unbiased)
+//     twice from a snapshot of its start: first for T, then to scatter the
+//     gradients; no per-path memory is kept.
+//   Both: dL/dn = sum over paths of (1/(n+1) + ln cos theta_0) * L_p (score
+//     function of the cos^n source).
+template <int M>
+__global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const TraceParams p) {
   const SceneView& s = p.s;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -175,6 +200,33 @@ __global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceP
   const uint64_t nrays = p.ray_end - p.ray_begin;
   const double lower = p.roulette_threshold * 1.0f;
   const double renew = p.roulette_weight * 1.0f;
+  // adjoint state
+  double wd = 0.0, lp = 0.0, score = 0.0, acc_s = 0.0, acc_n = 0.0, seg_t = 0.0, seg_p = 0.0;
+  double pa = 0.0, psum = 0.0, ncoll = 0.0;
+  const bool unbiased = p.adj_unbiased != 0;
+  int sub = 0;
+  f3 so = o, sd = d;
+  float sw = 1.0f;
+  uint32_t sk = 0, snseg = 0;
+  auto snapshot = [&]() {
+    so = o; sd = d; sw = w; sk = k; snseg = nseg;
+    seg_t = 0.0; seg_p = 0.0; sub = 0;
+  };
+  // end of a path; in the field replay the first pass of a stretch restarts it
+  auto path_end = [&]() -> bool {
+    if (M == kModeAdjField && sub == 0) {
+      o = so; d = sd; w = sw; k = sk; nseg = snseg;
+      seg_p = 0.0; sub = 1;
+      return true;
+    }
+    if (M == kModeAdjGlobal && unbiased) {
+      double ds = pa;
+      if (p.sticking < 1.0f) ds -= (ncoll * lp - psum) / (1.0 - (double)p.sticking);
+      acc_s += ds;
+    }
+    if (M != kModeForward) acc_n += score * lp;
+    return false;
+  };
   for (uint32_t iter = 0;; ++iter) {
     if (!exhausted) {
       const unsigned need = __ballot_sync(kFull, !active);
@@ -198,6 +250,15 @@ __global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceP
             k = 0;
             nseg = 0;
             active = true;
+            if (M != kModeForward) {
+              score = p.adj_inv_n1 + log(-(double)d.z);
+              lp = 0.0;
+              wd = 0.0;
+              pa = 0.0;
+              psum = 0.0;
+              ncoll = 0.0;
+              if (M == kModeAdjField) snapshot();
+            }
           }
         }
       }
@@ -216,7 +277,7 @@ __global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceP
     // ---- one segment (tracer.hpp:169-279) ----
     if (nseg == p.max_segments) {
       c_trunc += 1;
-      active = false;
+      active = path_end();
       continue;
     }
     nseg += 1;
@@ -239,7 +300,9 @@ __global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceP
       c_hit += 1;
       const float st = s.sticking_field ? __ldg(&s.sticking_field[hid]) : p.sticking;
       const float v = w * st;
-      deposit(p, hid, v);
+      double G = 0.0;
+      if (M == kModeForward) deposit(p, hid, v);
+      else G = __ldg(&p.adj_g[hid]);
       c_tot += 1;
       if (!(href & kTriBit) && s.nb_ptr) {  // tracer.hpp:339-383
         const int64_t q0 = __ldg(&s.nb_ptr[hid]), q1 = __ldg(&s.nb_ptr[hid + 1]);
@@ -248,26 +311,53 @@ __global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceP
           const float4 cr = __ldg(&s.disc_cr_by_id[nb]);
           const float4 nv = __ldg(&s.disc_n_by_id[nb]);
           if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
-            deposit(p, nb, v);
+            if (M == kModeForward) deposit(p, nb, v);
+            else G += __ldg(&p.adj_g[nb]);
             c_tot += 1;
             c_nb += 1;
           }
         }
       }
+      if (M == kModeAdjGlobal) {
+        lp += G * (double)v;
+        if (unbiased) {
+          pa += G * (double)w;
+          psum += lp;
+          ncoll += 1.0;
+        } else {
+          const double dv = (double)w + (double)st * wd;
+          acc_s += G * dv;
+          wd -= dv;
+        }
+      } else if (M == kModeAdjField) {
+        const double gv = G * (double)v;
+        if (sub == 0) {
+          seg_t += gv;
+        } else {
+          seg_p += gv;
+          lp += gv;
+          double gr = G * (double)w;
+          if (st < 1.0f) gr -= (seg_t - seg_p) / (1.0 - (double)st);
+          atomicAdd(&p.adj_field[hid], gr);
+        }
+      }
       w = w - v;
       if (w == 0.0f) {
-        active = false;
+        active = path_end();
         continue;
       }
       const uint4 u = draw4(p.seed, id, k, p.job);
       // rejection_control::check_weight_reweight_or_kill (rejection_control.hpp:28-61)
+      bool reset = false;
       if (!((double)w >= lower)) {
         const double kill = 1.0f - (double)w / renew;
         if ((double)u.x < kill * 4294967296.0) {
-          active = false;
+          active = path_end();
           continue;
         }
         w = (float)renew;
+        reset = true;
+        if (M == kModeAdjGlobal) wd = 0.0;
       }
       const bool spec = p.reflection == RTG_REFLECT_SPECULAR ||
                         (p.reflection == RTG_REFLECT_MIXED &&
@@ -275,6 +365,14 @@ __global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceP
       d = spec ? specular_dir(n, d) : diffuse_dir(n, u.y, u.z);
       o = hp;
       k += 1;
+      if (M == kModeAdjField && reset && !unbiased) {
+        if (sub == 0) {  // the stretch is complete: trace it again to scatter
+          o = so; d = sd; w = sw; k = sk; nseg = snseg;
+          seg_p = 0.0; sub = 1;
+        } else {
+          snapshot();  // the next stretch starts after this re-emission
+        }
+      }
       continue;
     }
     if (axis >= 0) {  // boundary_x_y::process_hit (boundary_x_y.hpp:92-143)
@@ -291,7 +389,15 @@ __global__ void __launch_bounds__(kTraceThreads) trace_paths_kernel(const TraceP
       continue;
     }
     c_non += 1;
-    active = false;
+    active = path_end();
+  }
+  if (M != kModeForward) {
+    acc_s = warp_sum_d(acc_s);
+    acc_n = warp_sum_d(acc_n);
+    if (lane == 0) {
+      atomicAdd(&p.adj_scalars[0], acc_s);
+      atomicAdd(&p.adj_scalars[1], acc_n);
+    }
   }
   c_hit = warp_sum(c_hit);
   c_non = warp_sum(c_non);
@@ -352,16 +458,19 @@ SceneView scene_view(rtg_context* ctx) {
   return s;
 }
 
-int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st) {
+int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st, int mode) {
   int dev = ctx->device, sms = 0, per_sm = 0;
+  auto kern = mode == kModeAdjGlobal  ? trace_paths_kernel<kModeAdjGlobal>
+              : mode == kModeAdjField ? trace_paths_kernel<kModeAdjField>
+                                      : trace_paths_kernel<kModeForward>;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_paths_kernel, kTraceThreads, 0));
+  RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0));
   if (per_sm < 1) per_sm = 1;
   uint64_t nrays = p.ray_end - p.ray_begin;
   uint64_t blocks = (uint64_t)sms * per_sm;
   uint64_t need = (nrays + kTraceThreads - 1) / kTraceThreads;
   if (need < blocks) blocks = need > 0 ? need : 1;
-  trace_paths_kernel<<<(unsigned)blocks, kTraceThreads, 0, st>>>(p);
+  kern<<<(unsigned)blocks, kTraceThreads, 0, st>>>(p);
   RTG_CUDA(ctx, cudaGetLastError());
   return RTG_OK;
 }

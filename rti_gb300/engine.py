@@ -184,6 +184,35 @@ class Engine:
                                            _ptr(t, L._f32p)))
         return prim, t
 
+    def set_sticking_field_device(self, d_field: int, n: int, stream=None):
+        """Sticking field from a float32 device array at address d_field (None/0 clears)."""
+        s = None if stream is None else C.c_void_p(int(stream) if int(stream) != 0 else 1)
+        self._check(self._L.rtg_set_sticking_field_device(self._h, C.c_void_p(int(d_field or 0)) if d_field else None,
+                                                          int(n), s))
+
+    # -- adjoint ----------------------------------------------------------------
+    def adjoint(self, g, n_rays: int, seed: int = 0, unbiased: bool = True):
+        """dL/ds, dL/dn and (with a sticking field) dL/ds_j for L = sum_i g_i S1_i,
+        by replaying rays [0, n_rays) of the trace with `seed` (host arrays)."""
+        gg = np.ascontiguousarray(g, dtype=np.float64)
+        if len(gg) != self.num_primitives:
+            raise ValueError("g must have one entry per primitive")
+        field = np.zeros(len(gg))
+        ds, dn = C.c_double(), C.c_double()
+        est = L.RTG_ADJ_UNBIASED if unbiased else L.RTG_ADJ_HELD
+        self._check(self._L.rtg_adjoint_host(self._h, _ptr(gg, L._f64p), int(n_rays), int(seed), est,
+                                             _ptr(field, L._f64p), C.byref(ds), C.byref(dn)))
+        return ds.value, dn.value, field
+
+    def adjoint_device(self, d_g: int, ray_begin: int, ray_end: int, seed: int, d_field_grad: int, d_scalars: int,
+                       unbiased: bool = True, stream=None):
+        """rtg_adjoint on device arrays (addresses); adds into d_field_grad / d_scalars."""
+        s = None if stream is None else C.c_void_p(int(stream) if int(stream) != 0 else 1)
+        est = L.RTG_ADJ_UNBIASED if unbiased else L.RTG_ADJ_HELD
+        self._check(self._L.rtg_adjoint(self._h, C.c_void_p(int(d_g)), int(ray_begin), int(ray_end), int(seed), est,
+                                        C.c_void_p(int(d_field_grad)) if d_field_grad else None,
+                                        C.c_void_p(int(d_scalars)), s))
+
     # -- results --------------------------------------------------------------
     def mc_estimates(self) -> np.ndarray:
         out = np.zeros(self.num_primitives, dtype=np.float32)
