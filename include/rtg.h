@@ -214,6 +214,39 @@ typedef struct rtg_device_view {
 } rtg_device_view;
 RTG_API int rtg_get_device_view(rtg_context* ctx, rtg_device_view* view);
 
+/* Batches (no counterpart in rti, which traces one geometry per
+ * tracer::run, tracer.hpp:66-330; a batch replaces back-to-back runs).
+ * A batch is a list of jobs, each a surface (a context with geometry), a
+ * configuration (NULL = the context's), a ray count and a seed.  Job j's paths
+ * use the Philox stream (seed, job tag j), so its results do not depend on the
+ * other jobs or on how the batch is run.  rtg_batch_run traces all jobs in ONE
+ * persistent launch whose lanes draw ray ids over the concatenated ray ranges
+ * (use_graph != 0: the zeroing, the launch and the area kernels are captured
+ * into a CUDA graph on the first run and replayed afterwards);
+ * rtg_batch_run_sequential issues one plain launch per job, with the same
+ * results.  A job keeps the device addresses of its context's geometry as of
+ * rtg_batch_add: re-uploading a context's geometry (rtg_upload_*) needs a new
+ * batch; refits (rtg_update_*) and new values of a sticking field that was
+ * already set (same size) at rtg_batch_add are seen by later runs.
+ * The contexts must outlive the batch and must not trace while it runs. */
+typedef struct rtg_batch rtg_batch;
+RTG_API int rtg_batch_create(rtg_batch** out, int device);
+RTG_API int rtg_batch_destroy(rtg_batch* b);
+RTG_API const char* rtg_batch_last_error(const rtg_batch* b);
+RTG_API int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint64_t n_rays, uint64_t seed,
+                          int32_t* job_out);
+RTG_API int rtg_batch_num_jobs(const rtg_batch* b, int32_t* n);
+/* Enqueue on `stream` (NULL = the batch's own stream); returns without waiting. */
+RTG_API int rtg_batch_run(rtg_batch* b, int use_graph, void* stream);
+RTG_API int rtg_batch_run_sequential(rtg_batch* b, void* stream);
+/* Waits for the last run; *elapsed_ms = its device time (may be NULL). */
+RTG_API int rtg_batch_synchronize(rtg_batch* b, double* elapsed_ms);
+/* Job results (host buffers of the job's primitive count; any may be NULL):
+ * S1 (hit_accumulator.hpp:140-142), hit counts (:144-146), exposed areas. */
+RTG_API int rtg_batch_get_results(rtg_batch* b, int32_t job, double* s1, uint64_t* counts, float* areas);
+/* Counters over all jobs of the last run. */
+RTG_API int rtg_batch_get_tally(rtg_batch* b, rtg_tally* out);
+
 /* device::run in one call (device.hpp:82-107): host arrays in, normalised
  * smoothed estimates and hit counts out.  sticking_field may be NULL. */
 RTG_API int rtg_device_run(const float* points, const float* normals, const float* radii, int64_t n,

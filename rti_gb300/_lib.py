@@ -38,6 +38,9 @@ EXPORTS = [
     "rtg_get_exposed_areas", "rtg_get_relative_error", "rtg_get_vov", "rtg_get_tally",
     "rtg_get_neighbors", "rtg_get_device_view", "rtg_device_run", "rtg_get_mc_estimates_noalloc",
     "rtg_set_sticking_field_device", "rtg_adjoint", "rtg_adjoint_host",
+    "rtg_batch_create", "rtg_batch_destroy", "rtg_batch_last_error", "rtg_batch_add", "rtg_batch_num_jobs",
+    "rtg_batch_run", "rtg_batch_run_sequential", "rtg_batch_synchronize", "rtg_batch_get_results",
+    "rtg_batch_get_tally",
 ]
 
 RTG_ADJ_HELD = 0
@@ -138,6 +141,16 @@ def load(path: str | None = None):
         "rtg_get_device_view": (C.c_int, [_ctx, C.POINTER(RtgDeviceView)]),
         "rtg_device_run": (C.c_int, [_f32p, _f32p, _f32p, C.c_int64, C.POINTER(RtgConfig), _f32p, C.c_uint64,
                                      C.c_uint64, _f32p, _u64p, C.c_int]),
+        "rtg_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+        "rtg_batch_destroy": (C.c_int, [C.c_void_p]),
+        "rtg_batch_last_error": (C.c_char_p, [C.c_void_p]),
+        "rtg_batch_add": (C.c_int, [C.c_void_p, _ctx, C.POINTER(RtgConfig), C.c_uint64, C.c_uint64, _i32p]),
+        "rtg_batch_num_jobs": (C.c_int, [C.c_void_p, _i32p]),
+        "rtg_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+        "rtg_batch_run_sequential": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "rtg_batch_synchronize": (C.c_int, [C.c_void_p, _f64p]),
+        "rtg_batch_get_results": (C.c_int, [C.c_void_p, C.c_int32, _f64p, _u64p, _f32p]),
+        "rtg_batch_get_tally": (C.c_int, [C.c_void_p, C.POINTER(RtgTally)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -56,13 +56,13 @@ int alloc_results(rtg_context* ctx) {
 // The trace box: explicit, or rti's rule (device.hpp:86-92, 225-237,
 // point_cloud_disc_geometry.hpp:83-87): x/y = centre extents, z from the
 // lowest centre to the highest centre + 2 r_max (source plane).
-void resolve_box(rtg_context* ctx) {
-  const rtg_config& c = ctx->cfg;
-  const Geometry& g = ctx->g;
+}  // namespace
+
+void box_for(const rtg_config& c, const Geometry& g, float* box_lo, float* box_hi) {
   if (c.box_mode == RTG_BOX_EXPLICIT) {
     for (int a = 0; a < 3; ++a) {
-      ctx->box_lo[a] = c.box_lo[a];
-      ctx->box_hi[a] = c.box_hi[a];
+      box_lo[a] = c.box_lo[a];
+      box_hi[a] = c.box_hi[a];
     }
     return;
   }
@@ -80,11 +80,15 @@ void resolve_box(rtg_context* ctx) {
   float top = hi[2];
   if (g.nd > 0) top = (hi[2] + g.rmax) + g.rmax;
   for (int a = 0; a < 3; ++a) {
-    ctx->box_lo[a] = lo[a];
-    ctx->box_hi[a] = hi[a];
+    box_lo[a] = lo[a];
+    box_hi[a] = hi[a];
   }
-  ctx->box_hi[2] = top;
+  box_hi[2] = top;
 }
+
+namespace {
+
+void resolve_box(rtg_context* ctx) { box_for(ctx->cfg, ctx->g, ctx->box_lo, ctx->box_hi); }
 
 int upload_discs_impl(rtg_context* ctx, const float* pts, const float* nrm, const float* rad, int64_t n,
                       bool rebuild) {
@@ -172,16 +176,19 @@ int upload_triangles_impl(rtg_context* ctx, const float* vertices, const uint32_
   return RTG_OK;
 }
 
+}  // namespace
+
 // Checks the context and fills the kernel parameters of a trace (or of its
-// adjoint replay) of source rays [ray_begin, ray_end).
-int prepare_trace(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, TraceParams& p) {
+// adjoint replay) of source rays [ray_begin, ray_end) under configuration c
+// and trace box box_lo/box_hi; accumulators and counters are the context's.
+int prepare_trace_with(rtg_context* ctx, const rtg_config& c, const float* box_lo, const float* box_hi,
+                       uint64_t ray_begin, uint64_t ray_end, uint64_t seed, TraceParams& p) {
   if (ray_end < ray_begin) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "ray_end < ray_begin");
   const int64_t np = ctx->g.nd + ctx->g.nt;
   if (np == 0 || !ctx->g.nodes.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no geometry uploaded");
   RTG_TRY(use_device(ctx));
-  const rtg_config& c = ctx->cfg;
   for (int a = 0; a < 2; ++a)
-    if (!(ctx->box_lo[a] < ctx->box_hi[a]))
+    if (!(box_lo[a] < box_hi[a]))
       return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "degenerate x/y box (all discs on one line?)");
   *ctx->h_abort = 0;
   p = TraceParams{};
@@ -197,13 +204,13 @@ int prepare_trace(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64
   p.ray_end = ray_end;
   p.seed = seed;
   for (int a = 0; a < 3; ++a) {
-    p.box_lo[a] = ctx->box_lo[a];
-    p.box_hi[a] = ctx->box_hi[a];
+    p.box_lo[a] = box_lo[a];
+    p.box_hi[a] = box_hi[a];
   }
-  p.src_lo[0] = ctx->box_lo[0];
-  p.src_lo[1] = ctx->box_lo[1];
-  p.src_hi[0] = ctx->box_hi[0];
-  p.src_hi[1] = ctx->box_hi[1];
+  p.src_lo[0] = box_lo[0];
+  p.src_lo[1] = box_lo[1];
+  p.src_hi[0] = box_hi[0];
+  p.src_hi[1] = box_hi[1];
   p.tnear = c.tnear;
   p.sticking = c.sticking;
   p.source_exponent = c.source_exponent;
@@ -218,6 +225,12 @@ int prepare_trace(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64
   p.job = c.job;
   p.adj_inv_n1 = 1.0 / ((double)c.source_exponent + 1.0);
   return RTG_OK;
+}
+
+namespace {
+
+int prepare_trace(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, TraceParams& p) {
+  return prepare_trace_with(ctx, ctx->cfg, ctx->box_lo, ctx->box_hi, ray_begin, ray_end, seed, p);
 }
 
 int rebuild_all(rtg_context* ctx) {
@@ -382,7 +395,16 @@ int rtg_update_vertices(rtg_context* ctx, const float* vertices, int64_t nv) {
 
 int rtg_set_config(rtg_context* ctx, const rtg_config* cfg) {
   if (!ctx || !cfg) return RTG_ERR_INVALID_ARGUMENT;
-  const rtg_config& c = *cfg;
+  RTG_TRY(check_config(ctx, *cfg));
+  ctx->cfg = *cfg;
+  resolve_box(ctx);
+  return RTG_OK;
+}
+
+}  // extern "C"
+
+namespace rtg {
+int check_config(rtg_context* ctx, const rtg_config& c) {
   auto bad = [&](const char* m) { return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, m); };
   if ((c.x_bound != RTG_BOUND_REFLECTIVE && c.x_bound != RTG_BOUND_PERIODIC) ||
       (c.y_bound != RTG_BOUND_REFLECTIVE && c.y_bound != RTG_BOUND_PERIODIC))
@@ -401,10 +423,11 @@ int rtg_set_config(rtg_context* ctx, const rtg_config* cfg) {
       if (!(c.box_lo[a] < c.box_hi[a]) || !std::isfinite(c.box_lo[a]) || !std::isfinite(c.box_hi[a]))
         return bad("explicit box needs finite box_lo < box_hi");
   }
-  ctx->cfg = c;
-  resolve_box(ctx);
   return RTG_OK;
 }
+}  // namespace rtg
+
+extern "C" {
 
 int rtg_get_config(const rtg_context* ctx, rtg_config* cfg) {
   if (!ctx || !cfg) return RTG_ERR_INVALID_ARGUMENT;

@@ -1,0 +1,302 @@
+// rtg_batch.cu -- many (surface, species) traces in one persistent launch.
+//
+// A batch holds jobs: a surface (an rtg_context with its LBVH, neighbour lists
+// and sticking field), a configuration (sticking, source exponent, boundaries,
+// re-emission, box) and a ray count and seed.  Each job has its own
+// accumulators.  rtg_batch_run zeroes them, launches the batched path kernel
+// once -- its lanes draw global ray ids over the concatenated ray ranges of
+// all jobs, so the tail of one job overlaps the start of the next -- and
+// computes each job's exposed areas; optionally the whole sequence is captured
+// into a CUDA graph once and replayed.  rtg_batch_run_sequential traces the
+// same jobs with one plain launch each (the comparison), with identical
+// results: every job's paths use the job's own Philox stream (seed, job tag).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rtg_internal.cuh"
+
+namespace rtg {
+namespace {
+
+struct Job {
+  rtg_context* scene = nullptr;
+  rtg_config cfg{};
+  uint64_t n_rays = 0, seed = 0;
+  float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
+  DBuf<double> acc;              // S1 | S2 | S3 | S4
+  DBuf<unsigned long long> cnt;
+  DBuf<float> areas;
+  TraceParams p{};
+};
+
+}  // namespace
+}  // namespace rtg
+
+struct rtg_batch {
+  rtg_context aux;  // device, stream and error text of the batch (no geometry)
+  std::vector<rtg::Job> jobs;
+  rtg::DBuf<rtg::TraceParams> d_jobs;
+  rtg::DBuf<uint64_t> d_prefix;
+  uint64_t total_rays = 0;
+  bool tables_ready = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+using namespace rtg;
+
+namespace {
+
+void drop_graph(rtg_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+int build_tables(rtg_batch* b) {
+  rtg_context* ctx = &b->aux;
+  const int n = (int)b->jobs.size();
+  std::vector<TraceParams> h(n);
+  std::vector<uint64_t> prefix(n + 1, 0);
+  for (int j = 0; j < n; ++j) {
+    h[j] = b->jobs[j].p;
+    prefix[j + 1] = prefix[j] + b->jobs[j].n_rays;
+  }
+  b->total_rays = prefix[n];
+  RTG_TRY(dalloc(ctx, b->d_jobs, (size_t)(n > 0 ? n : 1), "batch job table"));
+  RTG_TRY(dalloc(ctx, b->d_prefix, (size_t)(n + 1), "batch prefix"));
+  RTG_CUDA(ctx, cudaMemcpy(b->d_jobs.p, h.data(), n * sizeof(TraceParams), cudaMemcpyHostToDevice));
+  RTG_CUDA(ctx, cudaMemcpy(b->d_prefix.p, prefix.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice));
+  b->tables_ready = true;
+  return RTG_OK;
+}
+
+// The batched sequence on stream st: zero, one launch, areas.
+int enqueue_batched(rtg_batch* b, cudaStream_t st) {
+  rtg_context* ctx = &b->aux;
+  for (Job& j : b->jobs) {
+    const int64_t np = j.scene->g.nd + j.scene->g.nt;
+    RTG_CUDA(ctx, cudaMemsetAsync(j.acc.p, 0, 4 * np * sizeof(double), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(j.cnt.p, 0, np * sizeof(unsigned long long), st));
+  }
+  RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
+  TraceParams p0{};
+  p0.tally = ctx->d_tally;
+  p0.abort_flag = nullptr;
+  if (b->total_rays > 0)
+    RTG_TRY(launch_trace_batched(ctx, p0, b->d_jobs.p, b->d_prefix.p, (int)b->jobs.size(), b->total_rays, st));
+  for (Job& j : b->jobs) RTG_TRY(compute_areas_into(j.scene, st, j.box_lo, j.box_hi, j.areas.p));
+  return RTG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rtg_batch_create(rtg_batch** out, int device) {
+  if (!out) return RTG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return RTG_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_batch* b = new rtg_batch();
+  b->aux.device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->aux.stream, cudaStreamNonBlocking) !=
+                                                  cudaSuccess ||
+      cudaMalloc((void**)&b->aux.d_tally, sizeof(DevTally)) != cudaSuccess || cudaEventCreate(&b->ev0) != cudaSuccess ||
+      cudaEventCreate(&b->ev1) != cudaSuccess) {
+    cudaGetLastError();
+    if (b->aux.d_tally) cudaFree(b->aux.d_tally);
+    if (b->aux.stream) cudaStreamDestroy(b->aux.stream);
+    delete b;
+    return RTG_ERR_CUDA;
+  }
+  *out = b;
+  return RTG_OK;
+}
+
+int rtg_batch_destroy(rtg_batch* b) {
+  if (!b) return RTG_OK;
+  cudaSetDevice(b->aux.device);
+  if (b->aux.stream) cudaStreamSynchronize(b->aux.stream);
+  drop_graph(b);
+  for (Job& j : b->jobs) {
+    dfree(j.acc);
+    dfree(j.cnt);
+    dfree(j.areas);
+  }
+  dfree(b->d_jobs);
+  dfree(b->d_prefix);
+  if (b->aux.d_tally) cudaFree(b->aux.d_tally);
+  b->aux.d_tally = nullptr;
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->aux.stream) cudaStreamDestroy(b->aux.stream);
+  b->aux.stream = nullptr;
+  delete b;
+  return RTG_OK;
+}
+
+const char* rtg_batch_last_error(const rtg_batch* b) { return b ? b->aux.err.c_str() : "null batch"; }
+
+int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint64_t n_rays, uint64_t seed,
+                  int32_t* job_out) {
+  if (!b || !scene) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = &b->aux;
+  if (scene->device != ctx->device) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "scene is on another device");
+  if (scene->g.nd + scene->g.nt == 0 || !scene->g.nodes.p)
+    return set_error(ctx, RTG_ERR_NO_GEOMETRY, "scene has no geometry");
+  if (b->jobs.size() >= 0x7FFFFFFF) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "too many jobs");
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  Job j;
+  j.scene = scene;
+  j.cfg = cfg ? *cfg : scene->cfg;
+  if (check_config(ctx, j.cfg) != RTG_OK) return RTG_ERR_INVALID_ARGUMENT;
+  j.cfg.job = (uint32_t)b->jobs.size();  // a Philox stream of its own
+  j.n_rays = n_rays;
+  j.seed = seed;
+  box_for(j.cfg, scene->g, j.box_lo, j.box_hi);
+  const int64_t np = scene->g.nd + scene->g.nt;
+  int rc = dalloc(ctx, j.acc, (size_t)(4 * np), "batch accumulators");
+  if (rc == RTG_OK) rc = dalloc(ctx, j.cnt, (size_t)np, "batch counts");
+  if (rc == RTG_OK) rc = dalloc(ctx, j.areas, (size_t)np, "batch areas");
+  if (rc == RTG_OK) {
+    rc = prepare_trace_with(scene, j.cfg, j.box_lo, j.box_hi, 0, n_rays, seed, j.p);
+    if (rc != RTG_OK) set_error(ctx, rc, rtg_last_error(scene));
+  }
+  if (rc != RTG_OK) {
+    dfree(j.acc);
+    dfree(j.cnt);
+    dfree(j.areas);
+    return rc;
+  }
+  j.p.s1 = j.acc.p;
+  j.p.s2 = j.acc.p + np;
+  j.p.s3 = j.acc.p + 2 * np;
+  j.p.s4 = j.acc.p + 3 * np;
+  j.p.cnt = j.cnt.p;
+  j.p.tally = ctx->d_tally;
+  j.p.abort_flag = nullptr;
+  b->jobs.push_back(j);
+  b->tables_ready = false;
+  drop_graph(b);
+  if (job_out) *job_out = (int32_t)(b->jobs.size() - 1);
+  return RTG_OK;
+}
+
+int rtg_batch_num_jobs(const rtg_batch* b, int32_t* n) {
+  if (!b || !n) return RTG_ERR_INVALID_ARGUMENT;
+  *n = (int32_t)b->jobs.size();
+  return RTG_OK;
+}
+
+int rtg_batch_run(rtg_batch* b, int use_graph, void* stream) {
+  if (!b) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = &b->aux;
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!b->tables_ready) RTG_TRY(build_tables(b));
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  RTG_CUDA(ctx, cudaEventRecord(b->ev0, st));
+  if (!use_graph) {
+    RTG_TRY(enqueue_batched(b, st));
+  } else {
+    if (!b->exec) {
+      // capture on the batch's own stream, then replay on `st`
+      cudaStream_t cs = ctx->stream;
+      RTG_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue_batched(b, cs);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(cs, &g);
+      if (rc != RTG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return check_cuda(ctx, e, "graph capture");
+      b->graph = g;
+      RTG_CUDA(ctx, cudaGraphInstantiate(&b->exec, b->graph, 0));
+    }
+    RTG_CUDA(ctx, cudaGraphLaunch(b->exec, st));
+  }
+  RTG_CUDA(ctx, cudaEventRecord(b->ev1, st));
+  return RTG_OK;
+}
+
+int rtg_batch_run_sequential(rtg_batch* b, void* stream) {
+  if (!b) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = &b->aux;
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  RTG_CUDA(ctx, cudaEventRecord(b->ev0, st));
+  RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
+  for (Job& j : b->jobs) {
+    const int64_t np = j.scene->g.nd + j.scene->g.nt;
+    RTG_CUDA(ctx, cudaMemsetAsync(j.acc.p, 0, 4 * np * sizeof(double), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(j.cnt.p, 0, np * sizeof(unsigned long long), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(&ctx->d_tally->next_ray, 0, sizeof(unsigned long long), st));
+    if (j.n_rays > 0) RTG_TRY(launch_trace(ctx, j.p, st, kModeForward));
+    RTG_TRY(compute_areas_into(j.scene, st, j.box_lo, j.box_hi, j.areas.p));
+  }
+  RTG_CUDA(ctx, cudaEventRecord(b->ev1, st));
+  return RTG_OK;
+}
+
+int rtg_batch_synchronize(rtg_batch* b, double* elapsed_ms) {
+  if (!b) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = &b->aux;
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  RTG_CUDA(ctx, cudaEventSynchronize(b->ev1));
+  float ms = 0.0f;
+  RTG_CUDA(ctx, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  if (elapsed_ms) *elapsed_ms = ms;
+  DevTally t;
+  RTG_CUDA(ctx, cudaMemcpy(&t, ctx->d_tally, sizeof t, cudaMemcpyDeviceToHost));
+  if (t.errors) return set_error(ctx, RTG_ERR_BUDGET, "a device-side traversal limit was reached");
+  return RTG_OK;
+}
+
+int rtg_batch_get_results(rtg_batch* b, int32_t job, double* s1, uint64_t* counts, float* areas) {
+  if (!b || job < 0 || job >= (int32_t)b->jobs.size()) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = &b->aux;
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  RTG_CUDA(ctx, cudaDeviceSynchronize());
+  Job& j = b->jobs[(size_t)job];
+  const int64_t np = j.scene->g.nd + j.scene->g.nt;
+  if (s1) RTG_CUDA(ctx, cudaMemcpy(s1, j.acc.p, np * sizeof(double), cudaMemcpyDeviceToHost));
+  if (counts) RTG_CUDA(ctx, cudaMemcpy(counts, j.cnt.p, np * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  if (areas) RTG_CUDA(ctx, cudaMemcpy(areas, j.areas.p, np * sizeof(float), cudaMemcpyDeviceToHost));
+  return RTG_OK;
+}
+
+int rtg_batch_get_tally(rtg_batch* b, rtg_tally* out) {
+  if (!b || !out) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = &b->aux;
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  RTG_CUDA(ctx, cudaDeviceSynchronize());
+  DevTally t;
+  RTG_CUDA(ctx, cudaMemcpy(&t, ctx->d_tally, sizeof t, cudaMemcpyDeviceToHost));
+  std::memset(out, 0, sizeof *out);
+  uint64_t rays = 0;
+  for (const Job& j : b->jobs) rays += j.n_rays;
+  out->num_rays = rays;
+  out->hitc = t.hitc;
+  out->nonhitc = t.nonhitc;
+  out->total = t.total;
+  out->segments = t.segments;
+  out->truncated = t.truncated;
+  out->nb_deposits = t.nb_deposits;
+  out->errors = t.errors;
+  float ms = 0.0f;
+  if (cudaEventElapsedTime(&ms, b->ev0, b->ev1) == cudaSuccess) out->trace_ms = ms;
+  cudaGetLastError();
+  return RTG_OK;
+}
+
+}  // extern "C"

@@ -169,7 +169,15 @@ int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float t
                        float* d_t, cudaStream_t st);
 SceneView scene_view(rtg_context* ctx);
 
+int launch_trace_batched(rtg_context* ctx, const TraceParams& p0, const TraceParams* d_jobs, const uint64_t* d_prefix,
+                         int njobs, uint64_t total_rays, cudaStream_t st);
+int compute_areas_into(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi, float* out);
+
 // api.cu helpers
+int check_config(rtg_context* ctx, const rtg_config& c);
+void box_for(const rtg_config& c, const Geometry& g, float* box_lo, float* box_hi);
+int prepare_trace_with(rtg_context* ctx, const rtg_config& c, const float* box_lo, const float* box_hi,
+                       uint64_t ray_begin, uint64_t ray_end, uint64_t seed, TraceParams& p);
 int set_error(rtg_context* ctx, int code, const std::string& msg);
 int check_cuda(rtg_context* ctx, cudaError_t e, const char* what);
 template <typename T>

@@ -414,14 +414,18 @@ int build_neighbors(rtg_context* ctx) {
   return rc;
 }
 
-int compute_areas(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi) {
+int compute_areas_into(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi, float* out) {
   Geometry& g = ctx->g;
   const int64_t np = g.nd + g.nt;
   DBBI dbbi = make_dbbi(box_lo[0], box_lo[1], box_hi[0], box_hi[1]);
   area_kernel<<<blocks_for(np, 256), 256, 0, st>>>(g.disc_cr_by_id.p, g.disc_n_by_id.p, g.nd, g.tri_v.p,
-                                                   g.tri_idx.p, g.nt, dbbi, ctx->areas.p);
+                                                   g.tri_idx.p, g.nt, dbbi, out);
   RTG_CUDA(ctx, cudaGetLastError());
   return RTG_OK;
+}
+
+int compute_areas(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi) {
+  return compute_areas_into(ctx, st, box_lo, box_hi, ctx->areas.p);
 }
 
 int finalize_estimates(rtg_context* ctx, cudaStream_t st) {

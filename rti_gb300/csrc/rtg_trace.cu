@@ -186,9 +186,15 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 //     gradients; no per-path memory is kept.
 //   Both: dL/dn = sum over paths of (1/(n+1) + ln cos theta_0) * L_p (score
 //     function of the cos^n source).
-template <int M>
-__global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const TraceParams p) {
-  const SceneView& s = p.s;
+// Batched = true: lanes take global ray ids over the concatenated ray ranges
+// of `njobs` jobs (prefix[j] = first global id of job j) and trace each with
+// its job's parameters (scene, configuration, accumulators); the counters and
+// the abort flag are the batch's (p0).
+template <int M, bool Batched>
+__global__ void __launch_bounds__(kTraceThreads, 8)
+    trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
+                       const uint64_t* __restrict__ prefix, int njobs) {
+  const TraceParams* pp = &p0;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   unsigned long long c_hit = 0, c_non = 0, c_tot = 0, c_seg = 0, c_trunc = 0, c_nb = 0, c_err = 0;
@@ -197,13 +203,11 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
   f3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
   float w = 1.0f;
   uint32_t k = 0, nseg = 0;
-  const uint64_t nrays = p.ray_end - p.ray_begin;
-  const double lower = p.roulette_threshold * 1.0f;
-  const double renew = p.roulette_weight * 1.0f;
+  const uint64_t nrays = Batched ? prefix[njobs] : p0.ray_end - p0.ray_begin;
   // adjoint state
   double wd = 0.0, lp = 0.0, score = 0.0, acc_s = 0.0, acc_n = 0.0, seg_t = 0.0, seg_p = 0.0;
   double pa = 0.0, psum = 0.0, ncoll = 0.0;
-  const bool unbiased = p.adj_unbiased != 0;
+  const bool unbiased = p0.adj_unbiased != 0;
   int sub = 0;
   f3 so = o, sd = d;
   float sw = 1.0f;
@@ -221,7 +225,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
     }
     if (M == kModeAdjGlobal && unbiased) {
       double ds = pa;
-      if (p.sticking < 1.0f) ds -= (ncoll * lp - psum) / (1.0 - (double)p.sticking);
+      if (pp->sticking < 1.0f) ds -= (ncoll * lp - psum) / (1.0 - (double)pp->sticking);
       acc_s += ds;
     }
     if (M != kModeForward) acc_n += score * lp;
@@ -233,25 +237,36 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
       if (need) {
         const int leader = __ffs(need) - 1;
         unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(&p.tally->next_ray, (unsigned long long)__popc(need));
+        if (lane == leader) base = atomicAdd(&p0.tally->next_ray, (unsigned long long)__popc(need));
         base = __shfl_sync(kFull, base, leader);
         if (base + __popc(need) >= nrays) exhausted = true;
         if (!active) {
           const uint64_t j = base + (uint64_t)__popc(need & lt_mask);
           if (j < nrays) {
-            id = p.ray_begin + j;
+            if (Batched) {
+              int lo = 0, hi = njobs - 1;  // last job whose first id <= j
+              while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (__ldg(&prefix[mid]) <= j) lo = mid;
+                else hi = mid - 1;
+              }
+              pp = jobs + lo;
+              id = pp->ray_begin + (j - __ldg(&prefix[lo]));
+            } else {
+              id = p0.ray_begin + j;
+            }
             // source.hpp:20-58 with rectangle_origin_z / (power_)cosine_direction_z
-            const uint4 u = draw4(p.seed, id, 0xFFFFFFFFu, p.job);
+            const uint4 u = draw4(pp->seed, id, 0xFFFFFFFFu, pp->job);
             const float r1 = u01_co(u.x), r2 = u01_co(u.y);
-            o = mk3(p.src_lo[0] + (p.src_hi[0] - p.src_lo[0]) * r1,
-                    p.src_lo[1] + (p.src_hi[1] - p.src_lo[1]) * r2, p.box_hi[2]);
-            d = source_dir(p.source_exponent, p.source_ee, u.z, u.w);
+            o = mk3(pp->src_lo[0] + (pp->src_hi[0] - pp->src_lo[0]) * r1,
+                    pp->src_lo[1] + (pp->src_hi[1] - pp->src_lo[1]) * r2, pp->box_hi[2]);
+            d = source_dir(pp->source_exponent, pp->source_ee, u.z, u.w);
             w = 1.0f;
             k = 0;
             nseg = 0;
             active = true;
             if (M != kModeForward) {
-              score = p.adj_inv_n1 + log(-(double)d.z);
+              score = pp->adj_inv_n1 + log(-(double)d.z);
               lp = 0.0;
               wd = 0.0;
               pa = 0.0;
@@ -264,18 +279,18 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
       }
     }
     if (!__any_sync(kFull, active)) break;
-    if ((iter & 255u) == 0u && p.abort_flag) {
+    if ((iter & 255u) == 0u && p0.abort_flag) {
       unsigned stop = 0;
-      if (lane == 0) stop = *p.abort_flag;
+      if (lane == 0) stop = *p0.abort_flag;
       stop = __shfl_sync(kFull, stop, 0);
       if (stop) {
-        if (lane == 0) atomicExch(&p.tally->abort_seen, 1u);
+        if (lane == 0) atomicExch(&p0.tally->abort_seen, 1u);
         break;
       }
     }
     if (!active) continue;
     // ---- one segment (tracer.hpp:169-279) ----
-    if (nseg == p.max_segments) {
+    if (nseg == pp->max_segments) {
       c_trunc += 1;
       active = path_end();
       continue;
@@ -285,12 +300,12 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
     float th, tb = 0.0f;
     int hid;
     uint32_t href;
-    const bool hit = closest_hit(s, o, d, p.tnear, th, hid, href, c_err);
-    const int axis = boundary_exit(p, o, d, tb);
+    const bool hit = closest_hit(pp->s, o, d, pp->tnear, th, hid, href, c_err);
+    const int axis = boundary_exit(*pp, o, d, tb);
     if (hit && (axis < 0 || th <= tb)) {
       float4 nn;
-      if (href & kTriBit) nn = __ldg(&s.tri_n[href & kSlotMask]);
-      else nn = __ldg(&s.disc_n[href & kSlotMask]);
+      if (href & kTriBit) nn = __ldg(&pp->s.tri_n[href & kSlotMask]);
+      else nn = __ldg(&pp->s.disc_n[href & kSlotMask]);
       const f3 n = mk3(nn.x, nn.y, nn.z);
       const f3 hp = mk3(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
       if (d.x * n.x + d.y * n.y + d.z * n.z > 0.0f) {  // back face: pass through (tracer.hpp:216-227)
@@ -298,21 +313,21 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
         continue;
       }
       c_hit += 1;
-      const float st = s.sticking_field ? __ldg(&s.sticking_field[hid]) : p.sticking;
+      const float st = pp->s.sticking_field ? __ldg(&pp->s.sticking_field[hid]) : pp->sticking;
       const float v = w * st;
       double G = 0.0;
-      if (M == kModeForward) deposit(p, hid, v);
-      else G = __ldg(&p.adj_g[hid]);
+      if (M == kModeForward) deposit(*pp, hid, v);
+      else G = __ldg(&pp->adj_g[hid]);
       c_tot += 1;
-      if (!(href & kTriBit) && s.nb_ptr) {  // tracer.hpp:339-383
-        const int64_t q0 = __ldg(&s.nb_ptr[hid]), q1 = __ldg(&s.nb_ptr[hid + 1]);
+      if (!(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
+        const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
         for (int64_t q = q0; q < q1; ++q) {
-          const int nb = __ldg(&s.nb_idx[q]);
-          const float4 cr = __ldg(&s.disc_cr_by_id[nb]);
-          const float4 nv = __ldg(&s.disc_n_by_id[nb]);
+          const int nb = __ldg(&pp->s.nb_idx[q]);
+          const float4 cr = __ldg(&pp->s.disc_cr_by_id[nb]);
+          const float4 nv = __ldg(&pp->s.disc_n_by_id[nb]);
           if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
-            if (M == kModeForward) deposit(p, nb, v);
-            else G += __ldg(&p.adj_g[nb]);
+            if (M == kModeForward) deposit(*pp, nb, v);
+            else G += __ldg(&pp->adj_g[nb]);
             c_tot += 1;
             c_nb += 1;
           }
@@ -338,7 +353,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
           lp += gv;
           double gr = G * (double)w;
           if (st < 1.0f) gr -= (seg_t - seg_p) / (1.0 - (double)st);
-          atomicAdd(&p.adj_field[hid], gr);
+          atomicAdd(&pp->adj_field[hid], gr);
         }
       }
       w = w - v;
@@ -346,9 +361,11 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
         active = path_end();
         continue;
       }
-      const uint4 u = draw4(p.seed, id, k, p.job);
+      const uint4 u = draw4(pp->seed, id, k, pp->job);
       // rejection_control::check_weight_reweight_or_kill (rejection_control.hpp:28-61)
       bool reset = false;
+      const double lower = pp->roulette_threshold * 1.0f;
+      const double renew = pp->roulette_weight * 1.0f;
       if (!((double)w >= lower)) {
         const double kill = 1.0f - (double)w / renew;
         if ((double)u.x < kill * 4294967296.0) {
@@ -359,9 +376,9 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
         reset = true;
         if (M == kModeAdjGlobal) wd = 0.0;
       }
-      const bool spec = p.reflection == RTG_REFLECT_SPECULAR ||
-                        (p.reflection == RTG_REFLECT_MIXED &&
-                         (double)u.w < (double)p.specular_fraction * 4294967296.0);
+      const bool spec = pp->reflection == RTG_REFLECT_SPECULAR ||
+                        (pp->reflection == RTG_REFLECT_MIXED &&
+                         (double)u.w < (double)pp->specular_fraction * 4294967296.0);
       d = spec ? specular_dir(n, d) : diffuse_dir(n, u.y, u.z);
       o = hp;
       k += 1;
@@ -377,10 +394,10 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
     }
     if (axis >= 0) {  // boundary_x_y::process_hit (boundary_x_y.hpp:92-143)
       f3 hp = mk3(o.x + d.x * tb, o.y + d.y * tb, o.z + d.z * tb);
-      const int periodic = axis == 0 ? p.x_periodic : p.y_periodic;
+      const int periodic = axis == 0 ? pp->x_periodic : pp->y_periodic;
       if (periodic) {
-        if (axis == 0) hp.x = d.x > 0.0f ? p.box_lo[0] : p.box_hi[0];
-        else hp.y = d.y > 0.0f ? p.box_lo[1] : p.box_hi[1];
+        if (axis == 0) hp.x = d.x > 0.0f ? pp->box_lo[0] : pp->box_hi[0];
+        else hp.y = d.y > 0.0f ? pp->box_lo[1] : pp->box_hi[1];
       } else {
         if (axis == 0) d.x = -d.x;
         else d.y = -d.y;
@@ -395,8 +412,8 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
     acc_s = warp_sum_d(acc_s);
     acc_n = warp_sum_d(acc_n);
     if (lane == 0) {
-      atomicAdd(&p.adj_scalars[0], acc_s);
-      atomicAdd(&p.adj_scalars[1], acc_n);
+      atomicAdd(&pp->adj_scalars[0], acc_s);
+      atomicAdd(&pp->adj_scalars[1], acc_n);
     }
   }
   c_hit = warp_sum(c_hit);
@@ -407,13 +424,13 @@ __global__ void __launch_bounds__(kTraceThreads, 8) trace_paths_kernel(const Tra
   c_nb = warp_sum(c_nb);
   c_err = warp_sum(c_err);
   if (lane == 0) {
-    atomicAdd(&p.tally->hitc, c_hit);
-    atomicAdd(&p.tally->nonhitc, c_non);
-    atomicAdd(&p.tally->total, c_tot);
-    atomicAdd(&p.tally->segments, c_seg);
-    atomicAdd(&p.tally->truncated, c_trunc);
-    atomicAdd(&p.tally->nb_deposits, c_nb);
-    atomicAdd(&p.tally->errors, c_err);
+    atomicAdd(&p0.tally->hitc, c_hit);
+    atomicAdd(&p0.tally->nonhitc, c_non);
+    atomicAdd(&p0.tally->total, c_tot);
+    atomicAdd(&p0.tally->segments, c_seg);
+    atomicAdd(&p0.tally->truncated, c_trunc);
+    atomicAdd(&p0.tally->nb_deposits, c_nb);
+    atomicAdd(&p0.tally->errors, c_err);
   }
 }
 
@@ -460,9 +477,9 @@ SceneView scene_view(rtg_context* ctx) {
 
 int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st, int mode) {
   int dev = ctx->device, sms = 0, per_sm = 0;
-  auto kern = mode == kModeAdjGlobal  ? trace_paths_kernel<kModeAdjGlobal>
-              : mode == kModeAdjField ? trace_paths_kernel<kModeAdjField>
-                                      : trace_paths_kernel<kModeForward>;
+  auto kern = mode == kModeAdjGlobal  ? trace_paths_kernel<kModeAdjGlobal, false>
+              : mode == kModeAdjField ? trace_paths_kernel<kModeAdjField, false>
+                                      : trace_paths_kernel<kModeForward, false>;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0));
   if (per_sm < 1) per_sm = 1;
@@ -470,7 +487,22 @@ int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st, int mo
   uint64_t blocks = (uint64_t)sms * per_sm;
   uint64_t need = (nrays + kTraceThreads - 1) / kTraceThreads;
   if (need < blocks) blocks = need > 0 ? need : 1;
-  kern<<<(unsigned)blocks, kTraceThreads, 0, st>>>(p);
+  kern<<<(unsigned)blocks, kTraceThreads, 0, st>>>(p, nullptr, nullptr, 0);
+  RTG_CUDA(ctx, cudaGetLastError());
+  return RTG_OK;
+}
+
+int launch_trace_batched(rtg_context* ctx, const TraceParams& p0, const TraceParams* d_jobs, const uint64_t* d_prefix,
+                         int njobs, uint64_t total_rays, cudaStream_t st) {
+  int sms = 0, per_sm = 0;
+  auto kern = trace_paths_kernel<kModeForward, true>;
+  RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0));
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = (uint64_t)sms * per_sm;
+  const uint64_t need = (total_rays + kTraceThreads - 1) / kTraceThreads;
+  if (need < blocks) blocks = need > 0 ? need : 1;
+  kern<<<(unsigned)blocks, kTraceThreads, 0, st>>>(p0, d_jobs, d_prefix, njobs);
   RTG_CUDA(ctx, cudaGetLastError());
   return RTG_OK;
 }

@@ -245,3 +245,35 @@ def cylinder_triangles(radius: float = 0.5, depth: float = 45.0, cell: float = 1
     cylinder has radius 0.5 and length 45): the hole mesh without jitter."""
     return hole_triangles(radius=radius, depth=depth, cell=cell, n_theta=n_theta, n_wall=n_wall, n_top=n_top,
                           n_bottom=n_bottom, jitter=0.0, seed=0, source_gap=source_gap)
+
+
+# (sticking, cosine exponent) of the three species of the batched workload
+BATCH_SPECIES = ((0.01, 1.0), (0.1, 5.0), (1.0, 50.0))
+
+
+def batch_instances(n: int = 64, seed: int = 0, min_discs: int = 10_000, max_discs: int = 500_000,
+                    aspect: tuple = (2.0, 20.0)) -> list:
+    """Ragged set of `n` disc surfaces for the batched workload: trenches and
+    holes alternating, aspect ratio (depth / opening) uniform in `aspect` and a
+    target disc count uniform in [min_discs, max_discs]; the grid spacing is
+    chosen so that the sampled surface has about that many discs
+    (trench in a 3x3 cell: N ~ 3 (3 + 2 AR) / s^2; hole of diameter 1 in a 2x2
+    cell: N ~ (4 + pi AR) / s^2)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        ar = float(rng.uniform(*aspect))
+        target = float(rng.uniform(min_discs, max_discs))
+        if i % 2 == 0:
+            s = math.sqrt(3.0 * (3.0 + 2.0 * ar) / target)
+            nx = max(4, int(round(3.0 / s)))
+            s = 3.0 / nx
+            surf = trench_discs(width=1.0, depth=ar, domain=3.0, spacing=s)
+        else:
+            s = math.sqrt((4.0 + math.pi * ar) / target)
+            nx = max(4, int(round(2.0 / s)))
+            s = 2.0 / nx
+            surf = hole_discs(radius=0.5, depth=ar, cell=2.0, spacing=s)
+        surf.meta.update({"aspect": ar, "target": int(target), "index": i})
+        out.append(surf)
+    return out
