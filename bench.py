@@ -16,6 +16,12 @@ reference: the CPU restatement of rti's tracer (oracle/) on all host cores,
 each step a bounded sample of the same workload.
 Under torchrun each rank traces its own ray range (weak scaling) and the
 per-primitive accumulators are summed across ranks with NCCL.
+
+Extra blocks of the ours line (rank 0, 1 GPU): `plain_gpu` = the same trace as
+a non-persistent launch (one thread per source ray); `adjoint` = the adjoint
+replay of the same trace; `batch` = 64 ragged trench/hole disc surfaces x 3
+species x 2e6 rays in one autotuned, graph-replayed launch against 192
+sequential plain launches and 192 sequential persistent launches.
 """
 from __future__ import annotations
 
@@ -183,6 +189,60 @@ class _CAI:
                                          "version": 3}
 
 
+def run_batch_block(args):
+    """64 ragged surfaces x 3 species, 2e6 rays per job: one batched launch vs
+    192 back-to-back launches (plain, and persistent)."""
+    from rti_gb300 import Engine, scenes
+    from rti_gb300 import _lib as L
+    from rti_gb300.batch import Batch
+    t0 = time.perf_counter()
+    inst = scenes.batch_instances(n=64, seed=0)
+    engines, b = [], Batch(0)
+    for s in inst:
+        e = Engine(0)
+        e.upload_discs(s.points, s.normals, s.radii)
+        e.configure(box=(s.box_lo, s.box_hi), x_bound=1, y_bound=1, reset=True)
+        engines.append(e)
+        for stick, expo in scenes.BATCH_SPECIES:
+            c = e.config()
+            c.sticking, c.source_exponent = stick, expo
+            b.add(e, args.batch_rays, seed=0, config=c)
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tuned, _ = b.autotune(0.02)
+    tune_s = time.perf_counter() - t0
+    rays = len(b) * args.batch_rays
+
+    def timed(fn, reps):
+        out = []
+        for _ in range(reps + 1):
+            fn()
+            out.append(b.synchronize())
+        return statistics.mean(out[1:])
+
+    batched_ms = timed(lambda: b.run(use_graph=True), 2)
+    tb = b.tally()
+    seq_ms = timed(b.run_sequential, 1)
+    for e in engines:
+        e.set_launch_config(scheduling=L.RTG_SCHED_PLAIN)
+    plain_ms = timed(b.run_sequential, 1)
+    tp = b.tally()
+    for e in engines:
+        e.close()
+    b.close()
+    ok = tb.segments == tp.segments and tb.hitc == tp.hitc and tb.errors == 0
+    return {"workload": "64 trench/hole disc surfaces (aspect U[2,20], discs U[1e4,5e5], seeded) x 3 species "
+                        "(s, n) in {(0.01,1), (0.1,5), (1,50)}, 2e6 rays per job, x/y periodic",
+            "jobs": 192, "discs_total": int(sum(s.n for s in inst)), "rays": rays,
+            "segments": tb.segments, "launch_config": tuned, "autotune_s": tune_s, "setup_s": setup_s,
+            "batched_graph_ms": batched_ms, "batched_rays_per_s": rays / batched_ms * 1e3,
+            "sequential_plain_ms": plain_ms, "sequential_plain_rays_per_s": rays / plain_ms * 1e3,
+            "sequential_persistent_ms": seq_ms, "sequential_persistent_rays_per_s": rays / seq_ms * 1e3,
+            "speedup_vs_plain_launches": plain_ms / batched_ms,
+            "speedup_vs_persistent_launches": seq_ms / batched_ms,
+            "same_results": bool(ok)}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -317,6 +377,31 @@ def run_ours(args):
                "adjoint_ms": adj_ms, "forward_ms": fwd_ms, "adjoint_over_forward": adj_ms / fwd_ms,
                "grad_evals_per_s": 1e3 / (fwd_ms + adj_ms), "rays_per_grad_eval": R}
 
+    # the plain GPU baseline: the same trace as a non-persistent launch
+    plain = None
+    if not args.no_plain:
+        from rti_gb300 import _lib as L
+        eng.set_launch_config(scheduling=L.RTG_SCHED_PLAIN)
+        pm = []
+        for k in range(args.warmup + 3):
+            p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            p0.record(stream)
+            eng.trace(R, seed=k, stream=stream.cuda_stream, ray_begin=rank * R)
+            p1.record(stream)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                pm.append(p0.elapsed_time(p1))
+        tp = eng.tally()
+        eng.set_launch_config()
+        plain = {"value": world * R / (statistics.mean(pm) / 1e3), "unit": UNIT, "ms_per_step": statistics.mean(pm),
+                 "what": "one thread per source ray, non-persistent launch of the same path code",
+                 "errors": tp.errors}
+
+    batch = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        batch = run_batch_block(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rays_s, _ = cpu_sample(h, args.cpu_rays, os.cpu_count() or 1)
@@ -328,6 +413,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f64 accumulators",
                 "data": "synthetic", "config": config_dict(h, R), "clocks": clocks, "roofline": roof,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps, "adjoint": adj,
+                "plain_gpu": plain, "batch": batch,
                 "wall_s_timed_region": wall,
                 "tally_per_step": {"segments": seg, "hitc": statistics.mean(t.hitc for t in tallies),
                                    "truncated": max(t.truncated for t in tallies),
@@ -351,6 +437,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-rays", type=int, default=2_000_000, help="rays per job of the batch block")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     from __graft_entry__ import build

@@ -102,6 +102,27 @@ typedef struct rtg_tally {
   double   kernel_ms;    /* device time of the path kernel alone in the last rtg_trace */
 } rtg_tally;
 
+/* How the paths are scheduled on the GPU (no counterpart in rti, whose
+ * OpenMP loop has no such knobs).  None of these changes a result: every
+ * path is the same Philox-indexed computation whichever lane runs it.
+ *   RTG_SCHED_MEGAKERNEL: one persistent kernel carries every path to its end;
+ *   RTG_SCHED_WAVEFRONT: paths wait in a queue in device memory and advance
+ *     one segment per pair of kernels (closest hit, then shading), with the
+ *     surviving paths compacted between segments (forward traces only; the
+ *     adjoint replays always use the megakernel);
+ *   RTG_SCHED_PLAIN: a non-persistent launch, one thread per source ray that
+ *     traces its path to the end (the plain GPU baseline; forward traces). */
+#define RTG_SCHED_MEGAKERNEL 0
+#define RTG_SCHED_WAVEFRONT 1
+#define RTG_SCHED_PLAIN 2
+typedef struct rtg_launch_config {
+  int32_t threads_per_block; /* 64, 128 or 256 */
+  int32_t packet;            /* 1..32: a warp takes new source rays when at least this many lanes are idle */
+  int32_t stack_depth;       /* traversal stack entries, 32, 64 or 256; 0 = the smallest that holds the
+                                tree (a smaller request than the tree needs is raised to that) */
+  int32_t scheduling;        /* RTG_SCHED_* */
+} rtg_launch_config;
+
 /* Fills *cfg with rti's defaults. */
 RTG_API void rtg_config_default(rtg_config* cfg);
 RTG_API int  rtg_abi_version(void);
@@ -136,6 +157,21 @@ RTG_API int rtg_get_box(const rtg_context* ctx, float* box_lo3, float* box_hi3);
 RTG_API int rtg_set_sticking(rtg_context* ctx, float sticking);
 /* per-primitive sticking (length = number of primitives); NULL clears it */
 RTG_API int rtg_set_sticking_field(rtg_context* ctx, const float* sticking, int64_t n);
+
+/* Launch configuration of the traces of a context (default: 128 threads,
+ * packet 1, automatic stack, megakernel). */
+RTG_API void rtg_launch_config_default(rtg_launch_config* lc);
+RTG_API int rtg_set_launch_config(rtg_context* ctx, const rtg_launch_config* lc);
+RTG_API int rtg_get_launch_config(const rtg_context* ctx, rtg_launch_config* lc);
+/* Internal nodes on the longest root-to-leaf path of the context's LBVH. */
+RTG_API int rtg_get_tree_depth(const rtg_context* ctx, int32_t* depth);
+/* Autotuner: times each candidate launch configuration (block size x packet
+ * x stack depth x scheduling) on source rays [0, sample_rays) with `seed`
+ * under the current surface and configuration, keeps the fastest as the
+ * context's launch configuration and returns it (best and best_rays_per_s
+ * may be NULL).  Leaves no trace results behind (trace again afterwards). */
+RTG_API int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
+                         double* best_rays_per_s);
 
 /* Traces source rays [0, n_rays) with Philox seed `seed` on `stream`
  * (a cudaStream_t, NULL = the context's stream).  Zeroes the accumulators,
@@ -246,6 +282,15 @@ RTG_API int rtg_batch_synchronize(rtg_batch* b, double* elapsed_ms);
 RTG_API int rtg_batch_get_results(rtg_batch* b, int32_t job, double* s1, uint64_t* counts, float* areas);
 /* Counters over all jobs of the last run. */
 RTG_API int rtg_batch_get_tally(rtg_batch* b, rtg_tally* out);
+/* Launch configuration of rtg_batch_run (rtg_batch_run_sequential uses each
+ * job's context configuration).  RTG_SCHED_WAVEFRONT is driven from the host
+ * and is never captured: with it, rtg_batch_run(use_graph != 0) runs uncaptured. */
+RTG_API int rtg_batch_set_launch_config(rtg_batch* b, const rtg_launch_config* lc);
+RTG_API int rtg_batch_get_launch_config(const rtg_batch* b, rtg_launch_config* lc);
+/* Autotuner of the batched launch: times the candidates on the first
+ * sample_fraction (0 < f <= 1) of every job's rays, keeps the fastest. */
+RTG_API int rtg_batch_autotune(rtg_batch* b, double sample_fraction, rtg_launch_config* best,
+                               double* best_rays_per_s);
 
 /* device::run in one call (device.hpp:82-107): host arrays in, normalised
  * smoothed estimates and hit counts out.  sticking_field may be NULL. */

@@ -40,11 +40,16 @@ EXPORTS = [
     "rtg_set_sticking_field_device", "rtg_adjoint", "rtg_adjoint_host",
     "rtg_batch_create", "rtg_batch_destroy", "rtg_batch_last_error", "rtg_batch_add", "rtg_batch_num_jobs",
     "rtg_batch_run", "rtg_batch_run_sequential", "rtg_batch_synchronize", "rtg_batch_get_results",
-    "rtg_batch_get_tally",
+    "rtg_batch_get_tally", "rtg_launch_config_default", "rtg_set_launch_config", "rtg_get_launch_config",
+    "rtg_get_tree_depth", "rtg_autotune", "rtg_batch_set_launch_config", "rtg_batch_get_launch_config",
+    "rtg_batch_autotune",
 ]
 
 RTG_ADJ_HELD = 0
 RTG_ADJ_UNBIASED = 1
+RTG_SCHED_MEGAKERNEL = 0
+RTG_SCHED_WAVEFRONT = 1
+RTG_SCHED_PLAIN = 2
 
 
 class RtgConfig(C.Structure):
@@ -75,6 +80,14 @@ class RtgTally(C.Structure):
 class RtgDeviceView(C.Structure):
     _fields_ = [("s1", C.c_void_p), ("s2", C.c_void_p), ("s3", C.c_void_p), ("s4", C.c_void_p),
                 ("counts", C.c_void_p), ("areas", C.c_void_p), ("estimates", C.c_void_p), ("n", C.c_int64)]
+
+
+class RtgLaunchConfig(C.Structure):
+    _fields_ = [("threads_per_block", C.c_int32), ("packet", C.c_int32), ("stack_depth", C.c_int32),
+                ("scheduling", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class RtgError(RuntimeError):
@@ -151,6 +164,14 @@ def load(path: str | None = None):
         "rtg_batch_synchronize": (C.c_int, [C.c_void_p, _f64p]),
         "rtg_batch_get_results": (C.c_int, [C.c_void_p, C.c_int32, _f64p, _u64p, _f32p]),
         "rtg_batch_get_tally": (C.c_int, [C.c_void_p, C.POINTER(RtgTally)]),
+        "rtg_launch_config_default": (None, [C.POINTER(RtgLaunchConfig)]),
+        "rtg_set_launch_config": (C.c_int, [_ctx, C.POINTER(RtgLaunchConfig)]),
+        "rtg_get_launch_config": (C.c_int, [_ctx, C.POINTER(RtgLaunchConfig)]),
+        "rtg_get_tree_depth": (C.c_int, [_ctx, _i32p]),
+        "rtg_autotune": (C.c_int, [_ctx, C.c_uint64, C.c_uint64, C.POINTER(RtgLaunchConfig), _f64p]),
+        "rtg_batch_set_launch_config": (C.c_int, [C.c_void_p, C.POINTER(RtgLaunchConfig)]),
+        "rtg_batch_get_launch_config": (C.c_int, [C.c_void_p, C.POINTER(RtgLaunchConfig)]),
+        "rtg_batch_autotune": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(RtgLaunchConfig), _f64p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

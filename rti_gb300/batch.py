@@ -94,6 +94,25 @@ class Batch:
                                                   _ptr(areas, L._f32p)))
         return s1, cnt, areas
 
+    def set_launch_config(self, threads_per_block: int = 128, packet: int = 1, stack_depth: int = 0,
+                          scheduling: int = L.RTG_SCHED_MEGAKERNEL):
+        lc = L.RtgLaunchConfig(threads_per_block, packet, stack_depth, scheduling)
+        self._check(self._L.rtg_batch_set_launch_config(self._h, C.byref(lc)))
+
+    def launch_config(self) -> dict:
+        lc = L.RtgLaunchConfig()
+        self._check(self._L.rtg_batch_get_launch_config(self._h, C.byref(lc)))
+        return lc.as_dict()
+
+    def autotune(self, sample_fraction: float = 0.05):
+        """Times the candidate launch configurations of the batched launch on
+        the first ``sample_fraction`` of every job's rays and keeps the fastest;
+        returns (config dict, rays/s of the sample).  Run again afterwards."""
+        lc = L.RtgLaunchConfig()
+        r = C.c_double()
+        self._check(self._L.rtg_batch_autotune(self._h, float(sample_fraction), C.byref(lc), C.byref(r)))
+        return lc.as_dict(), r.value
+
     def tally(self) -> Tally:
         t = L.RtgTally()
         self._check(self._L.rtg_batch_get_tally(self._h, C.byref(t)))

@@ -19,7 +19,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librtg.so")
-SOURCES = ["rtg_api.cu", "rtg_batch.cu", "rtg_lbvh.cu", "rtg_noalloc.cu", "rtg_sort.cu", "rtg_surface.cu", "rtg_trace.cu"]
+SOURCES = ["rtg_api.cu", "rtg_batch.cu", "rtg_lbvh.cu", "rtg_noalloc.cu", "rtg_sort.cu", "rtg_surface.cu", "rtg_trace.cu", "rtg_trace_batched.cu",
+           "rtg_wavefront.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "-I", os.path.join(ROOT, "include")]

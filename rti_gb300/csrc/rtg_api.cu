@@ -321,6 +321,7 @@ int rtg_destroy(rtg_context* ctx) {
   dfree(g.refit_flags); dfree(g.nb_ptr); dfree(g.nb_idx);
   dfree(ctx->sticking_field); dfree(ctx->acc); dfree(ctx->cnt); dfree(ctx->areas); dfree(ctx->est);
   dfree(ctx->stat_tmp);
+  free_wavefront(ctx->wf);
   if (ctx->d_tally) cudaFree(ctx->d_tally);
   if (ctx->d_tally_adj) cudaFree(ctx->d_tally_adj);
   if (ctx->h_abort) cudaFreeHost(ctx->h_abort);
@@ -466,6 +467,94 @@ int rtg_set_sticking_field(rtg_context* ctx, const float* s, int64_t n) {
   RTG_TRY(dalloc(ctx, ctx->sticking_field, (size_t)n, "sticking field"));
   RTG_CUDA(ctx, cudaMemcpyAsync(ctx->sticking_field.p, s, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
   RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RTG_OK;
+}
+
+void rtg_launch_config_default(rtg_launch_config* lc) {
+  if (!lc) return;
+  lc->threads_per_block = 128;
+  lc->packet = 1;
+  lc->stack_depth = 0;
+  lc->scheduling = RTG_SCHED_MEGAKERNEL;
+}
+
+int rtg_set_launch_config(rtg_context* ctx, const rtg_launch_config* lc) {
+  if (!ctx || !lc) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(check_launch_config(ctx, *lc));
+  ctx->lc = *lc;
+  return RTG_OK;
+}
+
+int rtg_get_launch_config(const rtg_context* ctx, rtg_launch_config* lc) {
+  if (!ctx || !lc) return RTG_ERR_INVALID_ARGUMENT;
+  *lc = ctx->lc;
+  return RTG_OK;
+}
+
+int rtg_get_tree_depth(const rtg_context* ctx, int32_t* depth) {
+  if (!ctx || !depth) return RTG_ERR_INVALID_ARGUMENT;
+  *depth = ctx->g.depth;
+  return RTG_OK;
+}
+
+int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
+                 double* best_rays_per_s) {
+  if (!ctx || sample_rays == 0) return RTG_ERR_INVALID_ARGUMENT;
+  TraceParams p{};
+  RTG_TRY(prepare_trace(ctx, 0, sample_rays, seed, p));
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  cudaStream_t st = ctx->stream;
+  const rtg_launch_config keep = ctx->lc;
+  auto run = [&](const rtg_launch_config& lc, float& ms) -> int {
+    ctx->lc = lc;
+    RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * np * sizeof(double), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(ctx->cnt.p, 0, np * sizeof(unsigned long long), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->evk0, st));
+    RTG_TRY(launch_trace(ctx, p, st));
+    RTG_CUDA(ctx, cudaEventRecord(ctx->evk1, st));
+    RTG_CUDA(ctx, cudaEventSynchronize(ctx->evk1));
+    RTG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->evk0, ctx->evk1));
+    return RTG_OK;
+  };
+  std::vector<rtg_launch_config> cand;
+  for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT, RTG_SCHED_PLAIN})
+    for (int tpb : {64, 128, 256})
+      for (int packet : {1, 8, 32})
+        for (int stack : {0, 256}) {
+          if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
+          if (sched == RTG_SCHED_WAVEFRONT && (packet != 1 || tpb == 64)) continue;  // no refill in a wavefront
+          if (stack == 256 && stack_for(0, ctx->g.depth) == 256) continue;
+          cand.push_back(rtg_launch_config{tpb, packet, stack, sched});
+        }
+  std::vector<float> best_ms(cand.size(), 0.0f);
+  int rc = RTG_OK;
+  float ms = 0.0f;
+  for (size_t i = 0; i < cand.size() && rc == RTG_OK; ++i) {
+    rc = run(cand[i], ms);  // warm-up (and, for the wavefront, its queue allocation)
+    if (rc == RTG_OK) rc = run(cand[i], best_ms[i]);
+  }
+  // the three fastest again, keep each one's best time
+  std::vector<size_t> order(cand.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return best_ms[a] < best_ms[b]; });
+  for (size_t r = 0; r < 2 && rc == RTG_OK; ++r)
+    for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
+      rc = run(cand[order[q]], ms);
+      if (rc == RTG_OK && ms < best_ms[order[q]]) best_ms[order[q]] = ms;
+    }
+  ctx->traced = false;
+  ctx->finalized = false;
+  if (rc != RTG_OK) {
+    ctx->lc = keep;
+    return rc;
+  }
+  size_t bi = 0;
+  for (size_t i = 1; i < cand.size(); ++i)
+    if (best_ms[i] < best_ms[bi]) bi = i;
+  ctx->lc = cand[bi];
+  if (best) *best = cand[bi];
+  if (best_rays_per_s) *best_rays_per_s = best_ms[bi] > 0.0f ? sample_rays / (best_ms[bi] * 1e-3) : 0.0;
   return RTG_OK;
 }
 

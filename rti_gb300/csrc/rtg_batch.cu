@@ -12,6 +12,7 @@
 // results: every job's paths use the job's own Philox stream (seed, job tag).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -45,6 +46,7 @@ struct rtg_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int depth = 0;  // deepest LBVH among the jobs' surfaces
 };
 
 using namespace rtg;
@@ -76,8 +78,9 @@ int build_tables(rtg_batch* b) {
   return RTG_OK;
 }
 
-// The batched sequence on stream st: zero, one launch, areas.
-int enqueue_batched(rtg_batch* b, cudaStream_t st) {
+// The batched sequence on stream st: zero, one launch over the ray ranges in
+// `prefix` (total rays `total`), areas.
+int enqueue_batched(rtg_batch* b, cudaStream_t st, const uint64_t* prefix, uint64_t total) {
   rtg_context* ctx = &b->aux;
   for (Job& j : b->jobs) {
     const int64_t np = j.scene->g.nd + j.scene->g.nt;
@@ -88,8 +91,8 @@ int enqueue_batched(rtg_batch* b, cudaStream_t st) {
   TraceParams p0{};
   p0.tally = ctx->d_tally;
   p0.abort_flag = nullptr;
-  if (b->total_rays > 0)
-    RTG_TRY(launch_trace_batched(ctx, p0, b->d_jobs.p, b->d_prefix.p, (int)b->jobs.size(), b->total_rays, st));
+  if (total > 0)
+    RTG_TRY(launch_trace_batched(ctx, p0, b->d_jobs.p, prefix, (int)b->jobs.size(), total, st, ctx->lc, b->depth));
   for (Job& j : b->jobs) RTG_TRY(compute_areas_into(j.scene, st, j.box_lo, j.box_hi, j.areas.p));
   return RTG_OK;
 }
@@ -186,6 +189,7 @@ int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint6
   j.p.tally = ctx->d_tally;
   j.p.abort_flag = nullptr;
   b->jobs.push_back(j);
+  if (scene->g.depth > b->depth) b->depth = scene->g.depth;
   b->tables_ready = false;
   drop_graph(b);
   if (job_out) *job_out = (int32_t)(b->jobs.size() - 1);
@@ -205,14 +209,14 @@ int rtg_batch_run(rtg_batch* b, int use_graph, void* stream) {
   if (!b->tables_ready) RTG_TRY(build_tables(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   RTG_CUDA(ctx, cudaEventRecord(b->ev0, st));
-  if (!use_graph) {
-    RTG_TRY(enqueue_batched(b, st));
+  if (!use_graph || ctx->lc.scheduling == RTG_SCHED_WAVEFRONT) {  // a host-driven wavefront is not captured
+    RTG_TRY(enqueue_batched(b, st, b->d_prefix.p, b->total_rays));
   } else {
     if (!b->exec) {
       // capture on the batch's own stream, then replay on `st`
       cudaStream_t cs = ctx->stream;
       RTG_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      int rc = enqueue_batched(b, cs);
+      int rc = enqueue_batched(b, cs, b->d_prefix.p, b->total_rays);
       cudaGraph_t g = nullptr;
       cudaError_t e = cudaStreamEndCapture(cs, &g);
       if (rc != RTG_OK) {
@@ -241,7 +245,10 @@ int rtg_batch_run_sequential(rtg_batch* b, void* stream) {
     RTG_CUDA(ctx, cudaMemsetAsync(j.acc.p, 0, 4 * np * sizeof(double), st));
     RTG_CUDA(ctx, cudaMemsetAsync(j.cnt.p, 0, np * sizeof(unsigned long long), st));
     RTG_CUDA(ctx, cudaMemsetAsync(&ctx->d_tally->next_ray, 0, sizeof(unsigned long long), st));
-    if (j.n_rays > 0) RTG_TRY(launch_trace(ctx, j.p, st, kModeForward));
+    if (j.n_rays > 0) {
+      const int rc = launch_trace(j.scene, j.p, st, kModeForward);
+      if (rc != RTG_OK) return set_error(ctx, rc, std::string("job trace: ") + j.scene->err);
+    }
     RTG_TRY(compute_areas_into(j.scene, st, j.box_lo, j.box_hi, j.areas.p));
   }
   RTG_CUDA(ctx, cudaEventRecord(b->ev1, st));
@@ -296,6 +303,90 @@ int rtg_batch_get_tally(rtg_batch* b, rtg_tally* out) {
   float ms = 0.0f;
   if (cudaEventElapsedTime(&ms, b->ev0, b->ev1) == cudaSuccess) out->trace_ms = ms;
   cudaGetLastError();
+  return RTG_OK;
+}
+
+int rtg_batch_set_launch_config(rtg_batch* b, const rtg_launch_config* lc) {
+  if (!b || !lc) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(check_launch_config(&b->aux, *lc));
+  if (std::memcmp(lc, &b->aux.lc, sizeof *lc) != 0) drop_graph(b);
+  b->aux.lc = *lc;
+  return RTG_OK;
+}
+
+int rtg_batch_get_launch_config(const rtg_batch* b, rtg_launch_config* lc) {
+  if (!b || !lc) return RTG_ERR_INVALID_ARGUMENT;
+  *lc = b->aux.lc;
+  return RTG_OK;
+}
+
+int rtg_batch_autotune(rtg_batch* b, double fraction, rtg_launch_config* best, double* best_rays_per_s) {
+  if (!b || !(fraction > 0.0 && fraction <= 1.0)) return RTG_ERR_INVALID_ARGUMENT;
+  rtg_context* ctx = &b->aux;
+  RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!b->tables_ready) RTG_TRY(build_tables(b));
+  const int n = (int)b->jobs.size();
+  if (n == 0) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "empty batch");
+  // the first fraction of every job's rays
+  std::vector<uint64_t> prefix(n + 1, 0);
+  for (int j = 0; j < n; ++j) {
+    const uint64_t r = b->jobs[j].n_rays;
+    uint64_t s = (uint64_t)(r * fraction);
+    if (s == 0 && r > 0) s = 1;
+    prefix[j + 1] = prefix[j] + s;
+  }
+  const uint64_t total = prefix[n];
+  DBuf<uint64_t> dp;
+  RTG_TRY(dalloc(ctx, dp, (size_t)(n + 1), "sample prefix"));
+  cudaStream_t st = ctx->stream;
+  int rc = check_cuda(ctx, cudaMemcpy(dp.p, prefix.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice),
+                      "sample prefix");
+  const rtg_launch_config keep = ctx->lc;
+  auto run = [&](const rtg_launch_config& lc, float& ms) -> int {
+    ctx->lc = lc;
+    RTG_CUDA(ctx, cudaEventRecord(b->ev0, st));
+    RTG_TRY(enqueue_batched(b, st, dp.p, total));
+    RTG_CUDA(ctx, cudaEventRecord(b->ev1, st));
+    RTG_CUDA(ctx, cudaEventSynchronize(b->ev1));
+    RTG_CUDA(ctx, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    return RTG_OK;
+  };
+  std::vector<rtg_launch_config> cand;
+  for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT, RTG_SCHED_PLAIN})
+    for (int tpb : {64, 128, 256})
+      for (int packet : {1, 8, 32})
+        for (int stack : {0, 256}) {
+          if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
+          if (sched == RTG_SCHED_WAVEFRONT && (packet != 1 || tpb == 64)) continue;
+          if (stack == 256 && stack_for(0, b->depth) == 256) continue;
+          cand.push_back(rtg_launch_config{tpb, packet, stack, sched});
+        }
+  std::vector<float> tms(cand.size(), 0.0f);
+  float ms = 0.0f;
+  for (size_t i = 0; i < cand.size() && rc == RTG_OK; ++i) {
+    rc = run(cand[i], ms);
+    if (rc == RTG_OK) rc = run(cand[i], tms[i]);
+  }
+  std::vector<size_t> order(cand.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return tms[x] < tms[y]; });
+  for (int r = 0; r < 2 && rc == RTG_OK; ++r)
+    for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
+      rc = run(cand[order[q]], ms);
+      if (rc == RTG_OK && ms < tms[order[q]]) tms[order[q]] = ms;
+    }
+  dfree(dp);
+  if (rc != RTG_OK) {
+    ctx->lc = keep;
+    return rc;
+  }
+  size_t bi = 0;
+  for (size_t i = 1; i < cand.size(); ++i)
+    if (tms[i] < tms[bi]) bi = i;
+  if (std::memcmp(&cand[bi], &keep, sizeof keep) != 0) drop_graph(b);
+  ctx->lc = cand[bi];
+  if (best) *best = cand[bi];
+  if (best_rays_per_s) *best_rays_per_s = tms[bi] > 0.0f ? total / (tms[bi] * 1e-3) : 0.0;
   return RTG_OK;
 }
 

@@ -76,6 +76,8 @@ struct TraceParams {
   int32_t reflection;
   uint32_t max_segments;
   uint32_t job;
+  int32_t packet;  // a warp takes new source rays when at least this many lanes are idle
+  int32_t plain;   // 1: one source ray per thread, no refill (grid covers all rays)
   // adjoint replay (unused by the forward trace)
   const double* adj_g;     // dL/dS1 by primitive id
   double* adj_field;       // dL/ds_j by primitive id (sticking-field mode) or nullptr
@@ -120,6 +122,22 @@ struct Geometry {
   float cmin[3] = {0, 0, 0}, cmax[3] = {0, 0, 0};
   float rmax = 0.0f;
   float tri_min[3] = {0, 0, 0}, tri_max[3] = {0, 0, 0};
+  int32_t depth = 0;  // internal nodes on the longest root-to-leaf path
+};
+
+// Wavefront scheduling state (device buffers, lazily allocated).
+struct Wavefront {
+  DBuf<float4> ow[2];           // per path slot: (o.xyz, w)
+  DBuf<float4> dk[2];           // (d.xyz, bits of k)
+  DBuf<uint4> meta[2];          // (id lo, id hi, job, nseg)
+  DBuf<float> hit_t;
+  DBuf<int32_t> hit_id;
+  DBuf<uint32_t> hit_ref;
+  DBuf<unsigned long long> ctl;  // see rtg_wavefront.cu
+  DBuf<TraceParams> one_job;     // job table of a single (unbatched) trace
+  DBuf<uint64_t> one_prefix;
+  unsigned long long* h_ctl = nullptr;  // pinned copy of ctl
+  uint32_t capacity = 0;
 };
 
 }  // namespace rtg
@@ -145,6 +163,8 @@ struct rtg_context {
   bool traced = false;
   bool finalized = false;
   float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
+  rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL};
+  rtg::Wavefront wf;
   std::string err;
 };
 
@@ -163,14 +183,23 @@ int build_neighbors(rtg_context* ctx);
 int compute_areas(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi);
 int finalize_estimates(rtg_context* ctx, cudaStream_t st);
 int compute_stats(rtg_context* ctx, cudaStream_t st, uint64_t total, double* d_rel, double* d_vov);
-// trace.cu
+// trace.cu: a single trace with the context's launch configuration
 int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st, int mode = kModeForward);
 int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim,
                        float* d_t, cudaStream_t st);
 SceneView scene_view(rtg_context* ctx);
-
+// stack entries for a requested depth (0 = automatic) and a tree depth: 32, 64 or 256
+int stack_for(int requested, int tree_depth);
+int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc);
+// trace_batched.cu: the megakernel over a job table (forward only)
 int launch_trace_batched(rtg_context* ctx, const TraceParams& p0, const TraceParams* d_jobs, const uint64_t* d_prefix,
-                         int njobs, uint64_t total_rays, cudaStream_t st);
+                         int njobs, uint64_t total_rays, cudaStream_t st, const rtg_launch_config& lc,
+                         int tree_depth);
+// wavefront.cu: the same paths scheduled as extend/shade kernel pairs over a
+// path queue (forward only; host-driven loop, not capturable)
+int launch_wavefront(rtg_context* ctx, const TraceParams& p0, const TraceParams* d_jobs, const uint64_t* d_prefix,
+                     int njobs, uint64_t total_rays, cudaStream_t st, const rtg_launch_config& lc, int tree_depth);
+void free_wavefront(Wavefront& wf);
 int compute_areas_into(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi, float* out);
 
 // api.cu helpers

@@ -296,7 +296,48 @@ __global__ void single_leaf_kernel(const uint32_t* __restrict__ leaf_ref, const 
   nodes[0].d = make_uint4(r, r, 0u, 0u);
 }
 
+// Internal nodes from each leaf up to the root (bounded walk); the maximum
+// is the deepest stack a traversal can need.
+__global__ void depth_kernel(int64_t n, const uint32_t* __restrict__ parent, unsigned int* __restrict__ depth) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t node = parent[(n - 1) + i];
+  unsigned int d = 0;
+  for (int iter = 0; iter < 512; ++iter) {
+    if ((int64_t)node >= n - 1) {
+      d = 0xFFFFFFFFu;  // a broken link (the structural check reports it)
+      break;
+    }
+    d += 1;
+    if (node == 0) break;
+    node = parent[node];
+  }
+  atomicMax(depth, d);
+}
+
 inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+int tree_depth(rtg_context* ctx, cudaStream_t st) {
+  Geometry& g = ctx->g;
+  const int64_t np = g.nd + g.nt;
+  if (np < 2) {
+    g.depth = 1;
+    return RTG_OK;
+  }
+  DBuf<unsigned int> dd;
+  RTG_TRY(dalloc(ctx, dd, 1, "tree depth"));
+  unsigned int h = 0;
+  cudaMemsetAsync(dd.p, 0, sizeof(unsigned int), st);
+  depth_kernel<<<blocks_for(np, 256), 256, 0, st>>>(np, g.parent.p, dd.p);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dd.p, sizeof h, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  dfree(dd);
+  if (e != cudaSuccess) return check_cuda(ctx, e, "tree depth");
+  if (h > 256) return set_error(ctx, RTG_ERR_INTERNAL, "LBVH deeper than 256 levels");
+  g.depth = (int32_t)h;
+  return RTG_OK;
+}
 
 int validate_tree(rtg_context* ctx, cudaStream_t st) {
   Geometry& g = ctx->g;
@@ -430,6 +471,7 @@ int build_lbvh(rtg_context* ctx) {
       if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "karras"); break; }
       if ((rc = validate_tree(ctx, st)) != RTG_OK) break;
     }
+    if ((rc = tree_depth(ctx, st)) != RTG_OK) break;
     rc = run_slots_and_refit(ctx, nullptr, nullptr, st);
   } while (0);
   cudaStreamSynchronize(st);

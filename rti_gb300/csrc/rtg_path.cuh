@@ -1,0 +1,449 @@
+// rtg_path.cuh -- the persistent path-tracing kernel (a template included by
+// the translation units that instantiate it) and the closest-hit traversal.
+//
+// One thread carries one particle path at a time, as tracer::run does per
+// OpenMP iteration (tracer.hpp:160-280): source ray, closest hit, periodic or
+// reflective x/y box, back-face pass-through, sticking deposit on the hit
+// primitive and on every crossed overlapping neighbour disc, Russian
+// roulette, diffuse/specular re-emission.  Threads are persistent: when at
+// least `packet` lanes of a warp are idle, the warp takes that many next
+// source-ray ids from a global counter (one atomic per warp), so long and
+// short paths share the SIMD lanes.
+//
+// Closest hit = stack traversal of the two-box LBVH nodes; ties in t go to the
+// lower primitive id, and the node boxes are conservative, so the chosen hit
+// does not depend on the traversal order.  The stack holds STACK entries; a
+// tree deeper than that would overflow it (counted as an error), so the host
+// picks STACK from the tree depth.
+#pragma once
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "rtg_internal.cuh"
+#include "rtg_math.cuh"
+
+namespace rtg {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ float safe_inv(float d) {
+  if (fabsf(d) < 1e-30f) d = d < 0.0f ? -1e-30f : 1e-30f;
+  return 1.0f / d;
+}
+
+struct Ray {
+  f3 o, d, idr;
+};
+
+// Slab test of one child box; returns the entry distance in tn.
+__device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, float lz, float hz, const Ray& r,
+                                     float tmax, float& tn) {
+  float t0x = (lx - r.o.x) * r.idr.x, t1x = (hx - r.o.x) * r.idr.x;
+  float t0y = (ly - r.o.y) * r.idr.y, t1y = (hy - r.o.y) * r.idr.y;
+  float t0z = (lz - r.o.z) * r.idr.z, t1z = (hz - r.o.z) * r.idr.z;
+  tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
+  float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+  return tn <= tf * 1.0000005f && tn <= tmax * 1.0000005f + 1e-30f;
+}
+
+__device__ __forceinline__ void test_leaf(const SceneView& s, uint32_t ref, const Ray& r, float tnear, float& bt,
+                                          int& bid, uint32_t& bref) {
+  const uint32_t slot = ref & kSlotMask;
+  float t;
+  int id;
+  bool h;
+  if (ref & kTriBit) {
+    const float4 a = __ldg(&s.tri[3 * slot]);
+    const float4 b = __ldg(&s.tri[3 * slot + 1]);
+    const float4 c = __ldg(&s.tri[3 * slot + 2]);
+    id = __float_as_int(a.w);
+    h = tri_test(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), r.o, r.d, tnear, t);
+  } else {
+    const float4 cr = __ldg(&s.disc_cr[slot]);
+    const float4 nn = __ldg(&s.disc_n[slot]);
+    id = __float_as_int(nn.w);
+    h = disc_test(mk3(cr.x, cr.y, cr.z), cr.w, mk3(nn.x, nn.y, nn.z), r.o, r.d, tnear, t);
+  }
+  if (h && (t < bt || (t == bt && id < bid))) {
+    bt = t;
+    bid = id;
+    bref = ref;
+  }
+}
+
+// Closest primitive hit; returns false when nothing is hit.  errs counts
+// stack overflows and iteration-limit trips (both end the query).
+template <int STACK>
+__device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& bt, int& bid, uint32_t& bref,
+                            unsigned long long& errs) {
+  Ray r;
+  r.o = o;
+  r.d = d;
+  r.idr = mk3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+  bt = FLT_MAX;
+  bid = INT_MAX;
+  bref = 0xFFFFFFFFu;
+  uint32_t stack[STACK];
+  int sp = 0;
+  uint32_t cur = s.root;
+  const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
+  for (int64_t it = 0;; ++it) {
+    if (it > max_iter) {
+      errs += 1;
+      break;
+    }
+    const Node* nd = s.nodes + cur;
+    const float4 a = __ldg(&nd->a);
+    const float4 b = __ldg(&nd->b);
+    const float4 c = __ldg(&nd->c);
+    const uint4 ch = __ldg(&nd->d);
+    float tn0, tn1;
+    bool h0 = slab(a.x, a.y, b.x, b.y, c.x, c.y, r, bt, tn0);
+    bool h1 = slab(a.z, a.w, b.z, b.w, c.z, c.w, r, bt, tn1);
+    if (h0 && (ch.x & kLeafBit)) {
+      test_leaf(s, ch.x, r, tnear, bt, bid, bref);
+      h0 = false;
+    }
+    if (h1 && (ch.y & kLeafBit)) {
+      test_leaf(s, ch.y, r, tnear, bt, bid, bref);
+      h1 = false;
+    }
+    if (h0 && h1) {
+      uint32_t nearc = tn0 <= tn1 ? ch.x : ch.y;
+      uint32_t farc = tn0 <= tn1 ? ch.y : ch.x;
+      if (sp < STACK) {
+        stack[sp++] = farc;
+      } else {
+        errs += 1;
+      }
+      cur = nearc;
+    } else if (h0) {
+      cur = ch.x;
+    } else if (h1) {
+      cur = ch.y;
+    } else {
+      if (sp == 0) break;
+      cur = stack[--sp];
+    }
+  }
+  return bid != INT_MAX;
+}
+
+// Side-face exit of the x/y box: 0 = x face, 1 = y face, -1 = the ray leaves
+// through the top or bottom first (a miss).
+__device__ __forceinline__ int boundary_exit(const TraceParams& p, f3 o, f3 d, float& tb) {
+  float tx = FLT_MAX, ty = FLT_MAX, tz = FLT_MAX;
+  if (d.x > 0.0f) tx = (p.box_hi[0] - o.x) / d.x;
+  else if (d.x < 0.0f) tx = (p.box_lo[0] - o.x) / d.x;
+  if (d.y > 0.0f) ty = (p.box_hi[1] - o.y) / d.y;
+  else if (d.y < 0.0f) ty = (p.box_lo[1] - o.y) / d.y;
+  if (d.z > 0.0f) tz = (p.box_hi[2] - o.z) / d.z;
+  else if (d.z < 0.0f) tz = (p.box_lo[2] - o.z) / d.z;
+  const int axis = tx <= ty ? 0 : 1;
+  const float t = tx <= ty ? tx : ty;
+  if (!(t < FLT_MAX)) return -1;
+  if (!(t >= p.tnear)) return -1;
+  if (t > tz) return -1;
+  tb = t;
+  return axis;
+}
+
+// hit_accumulator::use (hit_accumulator.hpp:128-138)
+__device__ __forceinline__ void deposit(const TraceParams& p, int id, float v) {
+  const double dv = (double)v;
+  atomicAdd(&p.s1[id], dv);
+  atomicAdd(&p.s2[id], dv * v);
+  atomicAdd(&p.s3[id], dv * v * v);
+  atomicAdd(&p.s4[id], dv * v * v * v);
+  atomicAdd(&p.cnt[id], 1ull);
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+  return v;
+}
+
+// kModeForward traces and deposits.  The adjoint modes replay the same paths
+// and accumulate derivatives of L = sum_i g_i S1_i instead.  G_k = the sum of g
+// over the primitives that received deposit k, v_k = w_k s its weight,
+// P_k = sum_{m<=k} G_m v_m.
+//   held (adj_unbiased = 0): the roulette decisions are held as drawn (what
+//     central differences with common random numbers measure).  Within a
+//     stretch between roulette resets the weight is a product of (1 - s_e)
+//     factors, so dL/ds_j = sum over deposits k on j of G_k w_k - (T - P_k) /
+//     (1 - s_j), T the stretch total.  One global s: dv_k/ds = w_k + s w'_k,
+//     w'_{k+1} = w'_k - dv_k/ds, w' = 0 after a reset.
+//   unbiased (adj_unbiased = 1): adds the likelihood ratio of each roulette
+//     survival (probability w/0.3); T becomes the path total L_p.  One global
+//     s: dL/ds = sum_k G_k w_k - (K L_p - sum_k P_k)/(1 - s) over K deposits.
+//   kModeAdjField traces each stretch (held) or the whole path (unbiased)
+//     twice from a snapshot of its start: first for T, then to scatter the
+//     gradients; no per-path memory is kept.
+//   Both: dL/dn = sum over paths of (1/(n+1) + ln cos theta_0) * L_p (score
+//     function of the cos^n source).
+// Batched = true: lanes take global ray ids over the concatenated ray ranges
+// of `njobs` jobs (prefix[j] = first global id of job j) and trace each with
+// its job's parameters (scene, configuration, accumulators); the counters and
+// the abort flag are the batch's (p0).  TPB threads per block and 1024 / TPB
+// resident blocks per SM as the register target (64 registers per thread).
+template <int M, bool Batched, int TPB, int STACK>
+__global__ void __launch_bounds__(TPB, 1024 / TPB)
+    trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
+                       const uint64_t* __restrict__ prefix, int njobs) {
+  const TraceParams* pp = &p0;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  unsigned long long c_hit = 0, c_non = 0, c_tot = 0, c_seg = 0, c_trunc = 0, c_nb = 0, c_err = 0;
+  bool active = false, exhausted = false;
+  uint64_t id = 0;
+  f3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
+  float w = 1.0f;
+  uint32_t k = 0, nseg = 0;
+  const uint64_t nrays = Batched ? prefix[njobs] : p0.ray_end - p0.ray_begin;
+  // adjoint state
+  double wd = 0.0, lp = 0.0, score = 0.0, acc_s = 0.0, acc_n = 0.0, seg_t = 0.0, seg_p = 0.0;
+  double pa = 0.0, psum = 0.0, ncoll = 0.0;
+  const bool unbiased = p0.adj_unbiased != 0;
+  int sub = 0;
+  f3 so = o, sd = d;
+  float sw = 1.0f;
+  uint32_t sk = 0, snseg = 0;
+  auto snapshot = [&]() {
+    so = o; sd = d; sw = w; sk = k; snseg = nseg;
+    seg_t = 0.0; seg_p = 0.0; sub = 0;
+  };
+  // end of a path; in the field replay the first pass of a stretch restarts it
+  auto path_end = [&]() -> bool {
+    if (M == kModeAdjField && sub == 0) {
+      o = so; d = sd; w = sw; k = sk; nseg = snseg;
+      seg_p = 0.0; sub = 1;
+      return true;
+    }
+    if (M == kModeAdjGlobal && unbiased) {
+      double ds = pa;
+      if (pp->sticking < 1.0f) ds -= (ncoll * lp - psum) / (1.0 - (double)pp->sticking);
+      acc_s += ds;
+    }
+    if (M != kModeForward) acc_n += score * lp;
+    return false;
+  };
+  for (uint32_t iter = 0;; ++iter) {
+    if (!exhausted) {
+      const unsigned need = __ballot_sync(kFull, !active);
+      if (need && __popc(need) >= p0.packet) {
+        const int leader = __ffs(need) - 1;
+        unsigned long long base = 0;
+        if (p0.plain) {  // one source ray per thread (all lanes are idle on the first pass)
+          base = (unsigned long long)blockIdx.x * TPB + (threadIdx.x & ~31u);
+          exhausted = true;
+        } else {
+          if (lane == leader) base = atomicAdd(&p0.tally->next_ray, (unsigned long long)__popc(need));
+          base = __shfl_sync(kFull, base, leader);
+          if (base + __popc(need) >= nrays) exhausted = true;
+        }
+        if (!active) {
+          const uint64_t j = base + (uint64_t)__popc(need & lt_mask);
+          if (j < nrays) {
+            if (Batched) {
+              int lo = 0, hi = njobs - 1;  // last job whose first id <= j
+              while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (__ldg(&prefix[mid]) <= j) lo = mid;
+                else hi = mid - 1;
+              }
+              pp = jobs + lo;
+              id = pp->ray_begin + (j - __ldg(&prefix[lo]));
+            } else {
+              id = p0.ray_begin + j;
+            }
+            // source.hpp:20-58 with rectangle_origin_z / (power_)cosine_direction_z
+            const uint4 u = draw4(pp->seed, id, 0xFFFFFFFFu, pp->job);
+            const float r1 = u01_co(u.x), r2 = u01_co(u.y);
+            o = mk3(pp->src_lo[0] + (pp->src_hi[0] - pp->src_lo[0]) * r1,
+                    pp->src_lo[1] + (pp->src_hi[1] - pp->src_lo[1]) * r2, pp->box_hi[2]);
+            d = source_dir(pp->source_exponent, pp->source_ee, u.z, u.w);
+            w = 1.0f;
+            k = 0;
+            nseg = 0;
+            active = true;
+            if (M != kModeForward) {
+              score = pp->adj_inv_n1 + log(-(double)d.z);
+              lp = 0.0;
+              wd = 0.0;
+              pa = 0.0;
+              psum = 0.0;
+              ncoll = 0.0;
+              if (M == kModeAdjField) snapshot();
+            }
+          }
+        }
+      }
+    }
+    if (!__any_sync(kFull, active)) break;
+    if ((iter & 255u) == 0u && p0.abort_flag) {
+      unsigned stop = 0;
+      if (lane == 0) stop = *p0.abort_flag;
+      stop = __shfl_sync(kFull, stop, 0);
+      if (stop) {
+        if (lane == 0) atomicExch(&p0.tally->abort_seen, 1u);
+        break;
+      }
+    }
+    if (!active) continue;
+    // ---- one segment (tracer.hpp:169-279) ----
+    if (nseg == pp->max_segments) {
+      c_trunc += 1;
+      active = path_end();
+      continue;
+    }
+    nseg += 1;
+    c_seg += 1;
+    float th, tb = 0.0f;
+    int hid;
+    uint32_t href;
+    const bool hit = closest_hit<STACK>(pp->s, o, d, pp->tnear, th, hid, href, c_err);
+    const int axis = boundary_exit(*pp, o, d, tb);
+    if (hit && (axis < 0 || th <= tb)) {
+      float4 nn;
+      if (href & kTriBit) nn = __ldg(&pp->s.tri_n[href & kSlotMask]);
+      else nn = __ldg(&pp->s.disc_n[href & kSlotMask]);
+      const f3 n = mk3(nn.x, nn.y, nn.z);
+      const f3 hp = mk3(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
+      if (d.x * n.x + d.y * n.y + d.z * n.z > 0.0f) {  // back face: pass through (tracer.hpp:216-227)
+        o = hp;
+        continue;
+      }
+      c_hit += 1;
+      const float st = pp->s.sticking_field ? __ldg(&pp->s.sticking_field[hid]) : pp->sticking;
+      const float v = w * st;
+      double G = 0.0;
+      if (M == kModeForward) deposit(*pp, hid, v);
+      else G = __ldg(&pp->adj_g[hid]);
+      c_tot += 1;
+      if (!(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
+        const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
+        for (int64_t q = q0; q < q1; ++q) {
+          const int nb = __ldg(&pp->s.nb_idx[q]);
+          const float4 cr = __ldg(&pp->s.disc_cr_by_id[nb]);
+          const float4 nv = __ldg(&pp->s.disc_n_by_id[nb]);
+          if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
+            if (M == kModeForward) deposit(*pp, nb, v);
+            else G += __ldg(&pp->adj_g[nb]);
+            c_tot += 1;
+            c_nb += 1;
+          }
+        }
+      }
+      if (M == kModeAdjGlobal) {
+        lp += G * (double)v;
+        if (unbiased) {
+          pa += G * (double)w;
+          psum += lp;
+          ncoll += 1.0;
+        } else {
+          const double dv = (double)w + (double)st * wd;
+          acc_s += G * dv;
+          wd -= dv;
+        }
+      } else if (M == kModeAdjField) {
+        const double gv = G * (double)v;
+        if (sub == 0) {
+          seg_t += gv;
+        } else {
+          seg_p += gv;
+          lp += gv;
+          double gr = G * (double)w;
+          if (st < 1.0f) gr -= (seg_t - seg_p) / (1.0 - (double)st);
+          atomicAdd(&pp->adj_field[hid], gr);
+        }
+      }
+      w = w - v;
+      if (w == 0.0f) {
+        active = path_end();
+        continue;
+      }
+      const uint4 u = draw4(pp->seed, id, k, pp->job);
+      // rejection_control::check_weight_reweight_or_kill (rejection_control.hpp:28-61)
+      bool reset = false;
+      const double lower = pp->roulette_threshold * 1.0f;
+      const double renew = pp->roulette_weight * 1.0f;
+      if (!((double)w >= lower)) {
+        const double kill = 1.0f - (double)w / renew;
+        if ((double)u.x < kill * 4294967296.0) {
+          active = path_end();
+          continue;
+        }
+        w = (float)renew;
+        reset = true;
+        if (M == kModeAdjGlobal) wd = 0.0;
+      }
+      const bool spec = pp->reflection == RTG_REFLECT_SPECULAR ||
+                        (pp->reflection == RTG_REFLECT_MIXED &&
+                         (double)u.w < (double)pp->specular_fraction * 4294967296.0);
+      d = spec ? specular_dir(n, d) : diffuse_dir(n, u.y, u.z);
+      o = hp;
+      k += 1;
+      if (M == kModeAdjField && reset && !unbiased) {
+        if (sub == 0) {  // the stretch is complete: trace it again to scatter
+          o = so; d = sd; w = sw; k = sk; nseg = snseg;
+          seg_p = 0.0; sub = 1;
+        } else {
+          snapshot();  // the next stretch starts after this re-emission
+        }
+      }
+      continue;
+    }
+    if (axis >= 0) {  // boundary_x_y::process_hit (boundary_x_y.hpp:92-143)
+      f3 hp = mk3(o.x + d.x * tb, o.y + d.y * tb, o.z + d.z * tb);
+      const int periodic = axis == 0 ? pp->x_periodic : pp->y_periodic;
+      if (periodic) {
+        if (axis == 0) hp.x = d.x > 0.0f ? pp->box_lo[0] : pp->box_hi[0];
+        else hp.y = d.y > 0.0f ? pp->box_lo[1] : pp->box_hi[1];
+      } else {
+        if (axis == 0) d.x = -d.x;
+        else d.y = -d.y;
+      }
+      o = hp;
+      continue;
+    }
+    c_non += 1;
+    active = path_end();
+  }
+  if (M != kModeForward) {
+    acc_s = warp_sum_d(acc_s);
+    acc_n = warp_sum_d(acc_n);
+    if (lane == 0) {
+      atomicAdd(&pp->adj_scalars[0], acc_s);
+      atomicAdd(&pp->adj_scalars[1], acc_n);
+    }
+  }
+  c_hit = warp_sum(c_hit);
+  c_non = warp_sum(c_non);
+  c_tot = warp_sum(c_tot);
+  c_seg = warp_sum(c_seg);
+  c_trunc = warp_sum(c_trunc);
+  c_nb = warp_sum(c_nb);
+  c_err = warp_sum(c_err);
+  if (lane == 0) {
+    atomicAdd(&p0.tally->hitc, c_hit);
+    atomicAdd(&p0.tally->nonhitc, c_non);
+    atomicAdd(&p0.tally->total, c_tot);
+    atomicAdd(&p0.tally->segments, c_seg);
+    atomicAdd(&p0.tally->truncated, c_trunc);
+    atomicAdd(&p0.tally->nb_deposits, c_nb);
+    atomicAdd(&p0.tally->errors, c_err);
+  }
+}
+
+}  // namespace
+}  // namespace rtg

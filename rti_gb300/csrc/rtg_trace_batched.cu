@@ -1,0 +1,45 @@
+// rtg_trace_batched.cu -- the path kernel over a job table (rtg_batch_run):
+// lanes draw global ray ids over the concatenated ray ranges of all jobs.
+#include "rtg_path.cuh"
+
+namespace rtg {
+
+namespace {
+
+using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_t*, int);
+
+template <int TPB>
+PathKernel batched_kernel(int stack) {
+  if (stack <= 32) return trace_paths_kernel<kModeForward, true, TPB, 32>;
+  if (stack <= 64) return trace_paths_kernel<kModeForward, true, TPB, 64>;
+  return trace_paths_kernel<kModeForward, true, TPB, 256>;
+}
+
+}  // namespace
+
+int launch_trace_batched(rtg_context* ctx, const TraceParams& p0_in, const TraceParams* d_jobs,
+                         const uint64_t* d_prefix, int njobs, uint64_t total_rays, cudaStream_t st,
+                         const rtg_launch_config& lc, int tree_depth) {
+  if (lc.scheduling == RTG_SCHED_WAVEFRONT)
+    return launch_wavefront(ctx, p0_in, d_jobs, d_prefix, njobs, total_rays, st, lc, tree_depth);
+  const int stack = stack_for(lc.stack_depth, tree_depth);
+  TraceParams p0 = p0_in;
+  p0.packet = lc.packet;
+  p0.plain = lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
+  int tpb = lc.threads_per_block, sms = 0, per_sm = 0;
+  PathKernel kern = tpb == 64 ? batched_kernel<64>(stack) : tpb == 256 ? batched_kernel<256>(stack)
+                                                                       : batched_kernel<128>(stack);
+  if (tpb != 64 && tpb != 256) tpb = 128;
+  RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = (uint64_t)sms * per_sm;
+  const uint64_t need = (total_rays + tpb - 1) / tpb;
+  if (need < blocks || p0.plain) blocks = need > 0 ? need : 1;
+  if (blocks > 0x7FFFFFFFull) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "too many rays for a plain launch");
+  kern<<<(unsigned)blocks, tpb, 0, st>>>(p0, d_jobs, d_prefix, njobs);
+  RTG_CUDA(ctx, cudaGetLastError());
+  return RTG_OK;
+}
+
+}  // namespace rtg

@@ -157,6 +157,31 @@ class Engine:
         f = _f32(field, (-1,))
         self._check(self._L.rtg_set_sticking_field(self._h, _ptr(f, L._f32p), len(f)))
 
+    # -- scheduling -----------------------------------------------------------
+    def launch_config(self) -> L.RtgLaunchConfig:
+        lc = L.RtgLaunchConfig()
+        self._check(self._L.rtg_get_launch_config(self._h, C.byref(lc)))
+        return lc
+
+    def set_launch_config(self, threads_per_block: int = 128, packet: int = 1, stack_depth: int = 0,
+                          scheduling: int = L.RTG_SCHED_MEGAKERNEL):
+        lc = L.RtgLaunchConfig(threads_per_block, packet, stack_depth, scheduling)
+        self._check(self._L.rtg_set_launch_config(self._h, C.byref(lc)))
+
+    @property
+    def tree_depth(self) -> int:
+        d = C.c_int32()
+        self._check(self._L.rtg_get_tree_depth(self._h, C.byref(d)))
+        return d.value
+
+    def autotune(self, sample_rays: int, seed: int = 0):
+        """Times the candidate launch configurations on a sample trace and keeps
+        the fastest; returns (config dict, rays/s of the sample)."""
+        lc = L.RtgLaunchConfig()
+        r = C.c_double()
+        self._check(self._L.rtg_autotune(self._h, int(sample_rays), int(seed), C.byref(lc), C.byref(r)))
+        return lc.as_dict(), r.value
+
     # -- tracing --------------------------------------------------------------
     def trace(self, n_rays: int, seed: int = 0, stream=None, *, ray_begin: int = 0, accumulate: bool = False):
         """Enqueues source rays [ray_begin, ray_begin + n_rays); returns immediately.

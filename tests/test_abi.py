@@ -43,6 +43,18 @@ def test_null_arguments_are_rejected_without_a_device(rtg_lib):
     assert rtg_lib.rtg_set_config(None, None) == 1
     assert rtg_lib.rtg_trace(None, 10, 0, None) == 1
     assert rtg_lib.rtg_last_error(None) == b"null context"
+    assert rtg_lib.rtg_batch_create(None, 0) == 1
+    assert rtg_lib.rtg_batch_add(None, None, None, 1, 0, None) == 1
+    assert rtg_lib.rtg_autotune(None, 10, 0, None, None) == 1
+    assert rtg_lib.rtg_set_launch_config(None, None) == 1
+
+
+def test_launch_config_default(rtg_lib):
+    from rti_gb300 import _lib
+    lc = _lib.RtgLaunchConfig()
+    rtg_lib.rtg_launch_config_default(C.byref(lc))
+    assert lc.as_dict() == {"threads_per_block": 128, "packet": 1, "stack_depth": 0,
+                            "scheduling": _lib.RTG_SCHED_MEGAKERNEL}
 
 
 LAYOUT_C = r"""
@@ -59,6 +71,8 @@ int main(void) {
   F(rtg_tally, errors); F(rtg_tally, trace_ms); F(rtg_tally, kernel_ms);
   printf("rtg_device_view %zu\n", sizeof(rtg_device_view));
   F(rtg_device_view, estimates); F(rtg_device_view, n);
+  printf("rtg_launch_config %zu\n", sizeof(rtg_launch_config));
+  F(rtg_launch_config, packet); F(rtg_launch_config, stack_depth); F(rtg_launch_config, scheduling);
   return 0;
 }
 """
@@ -72,7 +86,8 @@ def test_struct_layout_matches_ctypes(tmp_path):
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                               check=True).stdout.split("\n") if line)
-    structs = {"rtg_config": _lib.RtgConfig, "rtg_tally": _lib.RtgTally, "rtg_device_view": _lib.RtgDeviceView}
+    structs = {"rtg_config": _lib.RtgConfig, "rtg_tally": _lib.RtgTally, "rtg_device_view": _lib.RtgDeviceView,
+               "rtg_launch_config": _lib.RtgLaunchConfig}
     for key, val in out.items():
         if "." in key:
             s, m = key.split(".")
