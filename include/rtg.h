@@ -237,6 +237,45 @@ RTG_API int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols,
  * The trace's status is not checked here (see rtg_get_tally). */
 RTG_API int rtg_get_mc_estimates_noalloc(rtg_context* ctx, float* d_out, void* stream);
 
+/* VTK XML output (rti io/vtp_writer.hpp:27-139, 392-413, without VTK): an
+ * ASCII PolyData file in the layout of rti's writer -- discs as vertex cells
+ * with cell arrays Normals, radius, value (S1), exposed-area, hitcnt,
+ * relative-error, variance-of-variance; triangles as polygon cells with the
+ * same result arrays; one string field array per metadata (key, value) pair.
+ * Cell i is primitive i.  hitcnt is written as UInt64 (rti: UInt32).
+ * rtg_write_vtp writes a traced context (synchronises; RTG_ERR_NO_GEOMETRY
+ * before the first trace); the _discs/_triangles/_mixed forms write host
+ * arrays (result arrays may be NULL to leave them out) and need no GPU. */
+RTG_API int rtg_write_vtp(rtg_context* ctx, const char* path, const char* const* meta_keys,
+                          const char* const* meta_values, int32_t n_meta);
+RTG_API int rtg_write_vtp_discs(const char* path, int64_t n, const float* points, const float* normals,
+                                const float* radii, const double* value, const uint64_t* hitcnt,
+                                const float* exposed_area, const double* relative_error, const double* vov,
+                                const char* const* meta_keys, const char* const* meta_values, int32_t n_meta);
+RTG_API int rtg_write_vtp_triangles(const char* path, int64_t nv, const float* vertices, int64_t nt,
+                                    const uint32_t* indices, const double* value, const uint64_t* hitcnt,
+                                    const float* exposed_area, const double* relative_error, const double* vov,
+                                    const char* const* meta_keys, const char* const* meta_values, int32_t n_meta);
+RTG_API int rtg_write_vtp_mixed(const char* path, int64_t nd, const float* points, const float* normals,
+                                const float* radii, int64_t nv, const float* vertices, int64_t nt,
+                                const uint32_t* indices, const double* value, const uint64_t* hitcnt,
+                                const float* exposed_area, const double* relative_error, const double* vov,
+                                const char* const* meta_keys, const char* const* meta_values, int32_t n_meta);
+
+/* VTK XML input (rti io/vtp_point_cloud_reader.hpp:23-95,
+ * io/vtp_triangle_reader.hpp:19-68, without VTK): PolyData or UnstructuredGrid,
+ * DataArrays in ascii, binary (base64) or appended (raw/base64) form,
+ * uncompressed or zlib-compressed (zlib builds).  No GPU needed.  Call once with
+ * NULL output arrays to get the sizes, then with arrays of those sizes.
+ * Point cloud: centres (n x 3), unit normals (n x 3, normalised as rti does),
+ * radii from the cell array "radius", else "sqrt-of-area" * sqrt(3)/2 * (1+1/32).
+ * Triangles: vertices (nv x 3) and the three-point cells (nt x 3).
+ * On failure `err` (err_len bytes, may be NULL) holds the reason. */
+RTG_API int rtg_read_point_cloud(const char* path, int64_t* n, float* points, float* normals, float* radii,
+                                 char* err, int32_t err_len);
+RTG_API int rtg_read_triangles(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices,
+                               char* err, int32_t err_len);
+
 /* Device-resident views (valid until the geometry changes). */
 typedef struct rtg_device_view {
   double*   s1;        /* S1..S4 are consecutive arrays of n doubles */

@@ -42,7 +42,8 @@ EXPORTS = [
     "rtg_batch_run", "rtg_batch_run_sequential", "rtg_batch_synchronize", "rtg_batch_get_results",
     "rtg_batch_get_tally", "rtg_launch_config_default", "rtg_set_launch_config", "rtg_get_launch_config",
     "rtg_get_tree_depth", "rtg_autotune", "rtg_batch_set_launch_config", "rtg_batch_get_launch_config",
-    "rtg_batch_autotune",
+    "rtg_batch_autotune", "rtg_write_vtp", "rtg_write_vtp_discs", "rtg_write_vtp_triangles", "rtg_write_vtp_mixed",
+    "rtg_read_point_cloud", "rtg_read_triangles",
 ]
 
 RTG_ADJ_HELD = 0
@@ -172,6 +173,17 @@ def load(path: str | None = None):
         "rtg_batch_set_launch_config": (C.c_int, [C.c_void_p, C.POINTER(RtgLaunchConfig)]),
         "rtg_batch_get_launch_config": (C.c_int, [C.c_void_p, C.POINTER(RtgLaunchConfig)]),
         "rtg_batch_autotune": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(RtgLaunchConfig), _f64p]),
+        "rtg_write_vtp": (C.c_int, [_ctx, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int32]),
+        "rtg_write_vtp_discs": (C.c_int, [C.c_char_p, C.c_int64, _f32p, _f32p, _f32p, _f64p, _u64p, _f32p, _f64p,
+                                          _f64p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int32]),
+        "rtg_write_vtp_triangles": (C.c_int, [C.c_char_p, C.c_int64, _f32p, C.c_int64, _u32p, _f64p, _u64p, _f32p,
+                                              _f64p, _f64p, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
+                                              C.c_int32]),
+        "rtg_write_vtp_mixed": (C.c_int, [C.c_char_p, C.c_int64, _f32p, _f32p, _f32p, C.c_int64, _f32p, C.c_int64,
+                                          _u32p, _f64p, _u64p, _f32p, _f64p, _f64p, C.POINTER(C.c_char_p),
+                                          C.POINTER(C.c_char_p), C.c_int32]),
+        "rtg_read_point_cloud": (C.c_int, [C.c_char_p, _i64p, _f32p, _f32p, _f32p, C.c_char_p, C.c_int32]),
+        "rtg_read_triangles": (C.c_int, [C.c_char_p, _i64p, _f32p, _i64p, _u32p, C.c_char_p, C.c_int32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

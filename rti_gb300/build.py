@@ -19,8 +19,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librtg.so")
-SOURCES = ["rtg_api.cu", "rtg_batch.cu", "rtg_lbvh.cu", "rtg_noalloc.cu", "rtg_sort.cu", "rtg_surface.cu", "rtg_trace.cu", "rtg_trace_batched.cu",
-           "rtg_wavefront.cu"]
+SOURCES = ["rtg_api.cu", "rtg_batch.cu", "rtg_lbvh.cu", "rtg_noalloc.cu", "rtg_sort.cu", "rtg_surface.cu", "rtg_trace.cu",
+           "rtg_trace_batched.cu", "rtg_vtk.cpp", "rtg_wavefront.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "-I", os.path.join(ROOT, "include")]
@@ -33,8 +33,26 @@ def nvcc() -> str:
     return exe
 
 
+def zlib_flags() -> tuple[list[str], list[str]]:
+    """(-D flag, link flag) when zlib's header and linkable library are present
+    (compressed VTK input); empty lists otherwise."""
+    inc = any(os.path.exists(os.path.join(d, "zlib.h")) for d in ("/usr/include", "/usr/local/include"))
+    lib = None
+    for d in ("/usr/lib/x86_64-linux-gnu", "/usr/lib/aarch64-linux-gnu", "/usr/lib64", "/usr/lib", "/lib64"):
+        for name in ("libz.so", "libz.so.1"):
+            if os.path.exists(os.path.join(d, name)):
+                lib = os.path.join(d, name)
+                break
+        if lib:
+            break
+    if inc and lib:
+        return ["-DRTG_WITH_ZLIB"], [lib]
+    return [], []
+
+
 def _deps() -> list[str]:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(HERE, "cli", "rtg_cli.cpp"))
     files.append(os.path.join(ROOT, "include", "rtg.h"))
     files.append(os.path.abspath(__file__))
     return files
@@ -53,9 +71,11 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     os.makedirs(BUILD, exist_ok=True)
     exe = nvcc()
     extra = list(extra or [])
+    zdef, zlink = zlib_flags()
+    extra += zdef
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = [exe, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -67,12 +87,27 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, *zlink, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
+
+
+def build_cli() -> str:
+    """The command-line driver (cli/rtg_cli.cpp) against librtg.so."""
+    gxx = shutil.which("g++") or "g++"
+    out = os.path.join(HERE, "rtg")
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
+    cmd = [gxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), os.path.join(HERE, "cli", "rtg_cli.cpp"),
+           "-L", HERE, "-lrtg", "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath-link,{cuda_lib}", "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed for the CLI:\n{r.stderr}")
+    os.replace(out + ".tmp", out)
+    return out
 
 
 if __name__ == "__main__":

@@ -843,6 +843,47 @@ int rtg_get_device_view(rtg_context* ctx, rtg_device_view* v) {
   return RTG_OK;
 }
 
+int rtg_write_vtp(rtg_context* ctx, const char* path, const char* const* meta_keys, const char* const* meta_values,
+                  int32_t n_meta) {
+  if (!ctx || !path || (n_meta > 0 && (!meta_keys || !meta_values))) return RTG_ERR_INVALID_ARGUMENT;
+  if (!ctx->traced) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "write_vtp: no trace results yet");
+  const Geometry& g = ctx->g;
+  const int64_t np = g.nd + g.nt;
+  std::vector<double> s1((size_t)np), rel((size_t)np), vov((size_t)np);
+  std::vector<uint64_t> cnt((size_t)np);
+  std::vector<float> area((size_t)np);
+  RTG_TRY(rtg_get_accumulators(ctx, s1.data(), nullptr, nullptr, nullptr));
+  RTG_TRY(rtg_get_hit_counts(ctx, cnt.data()));
+  RTG_TRY(rtg_get_exposed_areas(ctx, area.data()));
+  RTG_TRY(rtg_get_relative_error(ctx, rel.data()));
+  RTG_TRY(rtg_get_vov(ctx, vov.data()));
+  std::vector<float4> cr((size_t)g.nd), nn((size_t)g.nd), v4((size_t)g.nv);
+  std::vector<uint32_t> idx((size_t)(3 * g.nt));
+  if (g.nd > 0) {
+    RTG_CUDA(ctx, cudaMemcpy(cr.data(), g.disc_cr_by_id.p, g.nd * sizeof(float4), cudaMemcpyDeviceToHost));
+    RTG_CUDA(ctx, cudaMemcpy(nn.data(), g.disc_n_by_id.p, g.nd * sizeof(float4), cudaMemcpyDeviceToHost));
+  }
+  if (g.nt > 0) {
+    RTG_CUDA(ctx, cudaMemcpy(v4.data(), g.tri_v.p, g.nv * sizeof(float4), cudaMemcpyDeviceToHost));
+    RTG_CUDA(ctx, cudaMemcpy(idx.data(), g.tri_idx.p, 3 * g.nt * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  }
+  std::vector<float> pts((size_t)(3 * g.nd)), nrm((size_t)(3 * g.nd)), rad((size_t)g.nd), vtx((size_t)(3 * g.nv));
+  for (int64_t i = 0; i < g.nd; ++i) {
+    const float4 c = cr[(size_t)i], q = nn[(size_t)i];
+    pts[3 * i] = c.x; pts[3 * i + 1] = c.y; pts[3 * i + 2] = c.z;
+    nrm[3 * i] = q.x; nrm[3 * i + 1] = q.y; nrm[3 * i + 2] = q.z;
+    rad[(size_t)i] = c.w;
+  }
+  for (int64_t i = 0; i < g.nv; ++i) {
+    vtx[3 * i] = v4[(size_t)i].x; vtx[3 * i + 1] = v4[(size_t)i].y; vtx[3 * i + 2] = v4[(size_t)i].z;
+  }
+  const int rc = rtg_write_vtp_mixed(path, g.nd, pts.data(), nrm.data(), rad.data(), g.nt > 0 ? g.nv : 0, vtx.data(),
+                                     g.nt, idx.data(), s1.data(), cnt.data(), area.data(), rel.data(), vov.data(),
+                                     meta_keys, meta_values, n_meta);
+  if (rc != RTG_OK) return set_error(ctx, rc, std::string("write_vtp: cannot write ") + path);
+  return RTG_OK;
+}
+
 int rtg_device_run(const float* points, const float* normals, const float* radii, int64_t n, const rtg_config* cfg,
                    const float* sticking_field, uint64_t n_rays, uint64_t seed, float* est_out, uint64_t* cnt_out,
                    int device) {

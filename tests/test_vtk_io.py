@@ -1,0 +1,220 @@
+"""VTK XML output and input without VTK (no GPU needed).
+
+The writer follows rti's vtp_writer (io/vtp_writer.hpp: ASCII PolyData; cell
+arrays Normals, radius, value, exposed-area, hitcnt, relative-error,
+variance-of-variance; metadata as string field arrays); the readers follow
+io/vtp_point_cloud_reader.hpp and io/vtp_triangle_reader.hpp.  Input files in
+the other encodings VTK writes (inline base64, appended raw and base64, zlib
+blocks) are generated here from the VTK XML format description.
+"""
+import base64
+import os
+import struct
+import xml.etree.ElementTree as ET
+import zlib
+
+import numpy as np
+import pytest
+
+from rti_gb300 import RtgError, vtk
+
+RNG = np.random.default_rng(3)
+
+
+def _discs(n=7):
+    p = RNG.normal(size=(n, 3)).astype(np.float32)
+    nrm = RNG.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    r = RNG.uniform(0.01, 0.1, n).astype(np.float32)
+    return p, nrm.astype(np.float32), r
+
+
+def _cell_arrays(path):
+    root = ET.parse(path).getroot()
+    piece = root.find("PolyData/Piece")
+    out = {}
+    for da in piece.find("CellData"):
+        vals = np.array(da.text.split(), dtype=np.float64)
+        out[da.get("Name")] = (da.get("type"), int(da.get("NumberOfComponents", "1")), vals)
+    return root, piece, out
+
+
+def _field(root):
+    out = {}
+    for a in root.find("PolyData/FieldData"):
+        codes = [int(x) for x in a.text.split()]
+        assert codes[-1] == 0
+        out[a.get("Name")] = bytes(codes[:-1]).decode()
+    return out
+
+
+def test_disc_writer_layout_and_values(tmp_path):
+    p, n, r = _discs()
+    s1 = RNG.random(7)
+    cnt = RNG.integers(0, 2 ** 40, 7).astype(np.uint64)
+    area = RNG.random(7).astype(np.float32)
+    rel, vov = RNG.random(7), RNG.random(7)
+    f = tmp_path / "d.vtp"
+    meta = {"running-time[ns]": "123", "cmd": "rtg --infile a.vtp & <x>", "geo-name": "discs"}
+    vtk.write_vtp_discs(str(f), p, n, r, value=s1, hitcnt=cnt, exposed_area=area, relative_error=rel, vov=vov,
+                        metadata=meta)
+    root, piece, ca = _cell_arrays(f)
+    assert root.get("type") == "PolyData"
+    assert piece.get("NumberOfPoints") == "7" and piece.get("NumberOfVerts") == "7"
+    assert piece.get("NumberOfPolys") == "0"
+    assert piece.find("CellData").get("Normals") == "Normals"
+    assert list(ca) == ["Normals", "radius", "value", "exposed-area", "hitcnt", "relative-error",
+                        "variance-of-variance"]
+    assert ca["Normals"][1] == 3
+    np.testing.assert_array_equal(ca["Normals"][2].astype(np.float32), n.ravel())
+    np.testing.assert_array_equal(ca["radius"][2].astype(np.float32), r)
+    np.testing.assert_array_equal(ca["value"][2], s1)
+    np.testing.assert_array_equal(ca["exposed-area"][2].astype(np.float32), area)
+    assert ca["hitcnt"][0] == "UInt64"
+    assert [int(x) for x in ET.parse(f).getroot().find("PolyData/Piece/CellData")[4].text.split()] == \
+        [int(c) for c in cnt]
+    np.testing.assert_array_equal(ca["relative-error"][2], rel)
+    np.testing.assert_array_equal(ca["variance-of-variance"][2], vov)
+    pts = np.array(piece.find("Points/DataArray").text.split(), dtype=np.float32)
+    np.testing.assert_array_equal(pts, p.ravel())
+    verts = piece.find("Verts")
+    assert [int(x) for x in verts[0].text.split()] == list(range(7))
+    assert [int(x) for x in verts[1].text.split()] == list(range(1, 8))
+    assert _field(root) == meta
+
+
+def test_disc_round_trip_through_the_reader(tmp_path):
+    p, n, r = _discs(50)
+    f = tmp_path / "rt.vtp"
+    vtk.write_vtp_discs(str(f), p, n, r, value=np.zeros(50))
+    p2, n2, r2 = vtk.read_point_cloud(str(f))
+    np.testing.assert_array_equal(p2, p)
+    np.testing.assert_allclose(n2, n, rtol=0, atol=2e-7)
+    np.testing.assert_array_equal(r2, r)
+
+
+def test_triangle_writer_and_reader(tmp_path):
+    v = RNG.random((9, 3)).astype(np.float32)
+    t = np.array([[0, 1, 2], [3, 4, 5], [6, 7, 8], [0, 4, 8]], np.uint32)
+    f = tmp_path / "t.vtp"
+    vtk.write_vtp_triangles(str(f), v, t, value=np.arange(4.0), hitcnt=np.arange(4))
+    root, piece, ca = _cell_arrays(f)
+    assert piece.get("NumberOfPolys") == "4" and piece.get("NumberOfVerts") == "0"
+    assert list(ca) == ["value", "hitcnt"]
+    conn = [int(x) for x in piece.find("Polys")[0].text.split()]
+    assert conn == t.ravel().tolist()
+    v2, t2 = vtk.read_triangles(str(f))
+    np.testing.assert_array_equal(v2, v)
+    np.testing.assert_array_equal(t2, t)
+
+
+# ---- input in the other encodings -------------------------------------------
+
+def _enc_block(raw: bytes, header: str, compress: bool, b64: bool, joint: bool = True):
+    """One DataArray payload: VTK's [header][data] (or zlib blocks)."""
+    hf = "<I" if header == "UInt32" else "<Q"
+    if not compress:
+        head = struct.pack(hf, len(raw))
+        if not b64:
+            return head + raw
+        if joint:
+            return base64.b64encode(head + raw)
+        return base64.b64encode(head) + base64.b64encode(raw)
+    bs = 64
+    blocks = [raw[i:i + bs] for i in range(0, len(raw), bs)] or [b""]
+    comp = [zlib.compress(b) for b in blocks]
+    last = len(blocks[-1]) if len(blocks[-1]) != bs else 0
+    head = struct.pack(hf, len(blocks)) + struct.pack(hf, bs) + struct.pack(hf, last)
+    sizes = b"".join(struct.pack(hf, len(c)) for c in comp)
+    if not b64:
+        return head + sizes + b"".join(comp)
+    return base64.b64encode(head) + base64.b64encode(sizes) + base64.b64encode(b"".join(comp))
+
+
+def _write_encoded(path, arrays, mode, header="UInt32", compress=False, joint=True, unstructured=False,
+                   cells=None):
+    """arrays: list of (section, name, np array, ncomp); mode: binary | raw | base64."""
+    typ = {np.dtype(np.float32): "Float32", np.dtype(np.float64): "Float64", np.dtype(np.int64): "Int64",
+           np.dtype(np.int32): "Int32", np.dtype(np.uint8): "UInt8"}
+    kind = "UnstructuredGrid" if unstructured else "PolyData"
+    comp = ' compressor="vtkZLibDataCompressor"' if compress else ""
+    xml, app, off = [], b"", 0
+    xml.append(f'<?xml version="1.0"?>\n<VTKFile type="{kind}" version="1.0" byte_order="LittleEndian" '
+               f'header_type="{header}"{comp}>\n<{kind}>\n')
+    npts = len([a for a in arrays if a[0] == "Points"][0][2]) // 3
+    counts = f'NumberOfPoints="{npts}" ' + (f'NumberOfCells="{cells}"' if unstructured else 'NumberOfPolys="0"')
+    xml.append(f"<Piece {counts}>\n")
+    sections = []
+    for sec, *_ in arrays:
+        if sec not in sections:
+            sections.append(sec)
+    for sec in sections:
+        attr = ' Normals="nn"' if sec == "CellData" else ""
+        xml.append(f"<{sec}{attr}>\n")
+        for s2, name, a, ncomp in arrays:
+            if s2 != sec:
+                continue
+            payload = _enc_block(np.ascontiguousarray(a).tobytes(), header, compress, mode != "raw", joint)
+            head = f'<DataArray type="{typ[a.dtype]}" Name="{name}" NumberOfComponents="{ncomp}"'
+            if mode == "binary":
+                xml.append(f'{head} format="binary">\n{payload.decode()}\n</DataArray>\n')
+            else:
+                xml.append(f'{head} format="appended" offset="{off}"/>\n')
+                app += payload
+                off += len(payload)
+        xml.append(f"</{sec}>\n")
+    xml.append(f"</Piece>\n</{kind}>\n")
+    data = "".join(xml).encode()
+    if mode != "binary":
+        enc = "raw" if mode == "raw" else "base64"
+        data += f'<AppendedData encoding="{enc}">\n_'.encode() + app + b"\n</AppendedData>\n"
+    data += b"</VTKFile>\n"
+    open(path, "wb").write(data)
+
+
+@pytest.mark.parametrize("mode,header,compress,joint", [
+    ("binary", "UInt32", False, True), ("binary", "UInt64", False, False), ("raw", "UInt64", False, True),
+    ("base64", "UInt32", False, True), ("raw", "UInt32", True, True), ("binary", "UInt64", True, True)])
+def test_point_cloud_reader_encodings(tmp_path, mode, header, compress, joint):
+    p, n, r = _discs(40)
+    soa = (r / (np.sqrt(3.0) / 2 * (1 + 1 / 32))).astype(np.float64)
+    arrays = [("CellData", "nn", (n * 3.0).astype(np.float64).ravel(), 3), ("CellData", "sqrt-of-area", soa, 1),
+              ("Points", "Points", p.astype(np.float64).ravel(), 3)]
+    f = tmp_path / f"pc_{mode}_{header}_{compress}.vtp"
+    _write_encoded(f, arrays, mode, header, compress, joint)
+    try:
+        p2, n2, r2 = vtk.read_point_cloud(str(f))
+    except RtgError as e:
+        if compress and "zlib" in str(e):
+            pytest.skip("library built without zlib")
+        raise
+    np.testing.assert_array_equal(p2, p)
+    # normals of length 3 are normalised (utils.hpp is_normalized / normalize)
+    np.testing.assert_allclose(n2, n, rtol=0, atol=3e-7)
+    # radius = sqrt-of-area * sqrt(3)/2 * (1 + 1/32) (vtp_point_cloud_reader.hpp:75-81)
+    np.testing.assert_allclose(r2, (soa * np.sqrt(3.0) / 2 * (1 + 1 / 32)).astype(np.float32), rtol=1e-6)
+
+
+def test_unstructured_triangles_skip_other_cells(tmp_path):
+    v = RNG.random((8, 3)).astype(np.float32)
+    conn = np.array([0, 1, 2, 3, 4, 5, 6, 1, 2, 7], np.int64)  # triangle, quad, triangle
+    offs = np.array([3, 7, 10], np.int64)
+    types = np.array([5, 9, 5], np.uint8)
+    arrays = [("Points", "Points", v.ravel(), 3), ("Cells", "connectivity", conn, 1), ("Cells", "offsets", offs, 1),
+              ("Cells", "types", types, 1)]
+    f = tmp_path / "u.vtu"
+    _write_encoded(f, arrays, "raw", "UInt64", False, unstructured=True, cells=3)
+    v2, t2 = vtk.read_triangles(str(f))
+    np.testing.assert_array_equal(v2, v)
+    np.testing.assert_array_equal(t2, [[0, 1, 2], [1, 2, 7]])
+
+
+def test_reader_errors(tmp_path):
+    with pytest.raises(RtgError, match="cannot open"):
+        vtk.read_point_cloud(str(tmp_path / "missing.vtp"))
+    f = tmp_path / "nr.vtp"
+    p, n, _ = _discs(3)
+    _write_encoded(f, [("CellData", "nn", n.astype(np.float64).ravel(), 3),
+                       ("Points", "Points", p.astype(np.float64).ravel(), 3)], "binary")
+    with pytest.raises(RtgError, match="radius"):
+        vtk.read_point_cloud(str(f))
