@@ -21,7 +21,9 @@ Extra blocks of the ours line (rank 0, 1 GPU): `plain_gpu` = the same trace as
 a non-persistent launch (one thread per source ray); `adjoint` = the adjoint
 replay of the same trace; `batch` = 64 ragged trench/hole disc surfaces x 3
 species x 2e6 rays in one autotuned, graph-replayed launch against 192
-sequential plain launches and 192 sequential persistent launches.
+sequential plain launches and 192 sequential persistent launches;
+`rough_field` = 4.2 M discs with a per-disc sticking field, 1e8 rays, forward
+trace and the adjoint of all per-disc sticking gradients.
 """
 from __future__ import annotations
 
@@ -243,6 +245,58 @@ def run_batch_block(args):
             "same_results": bool(ok)}
 
 
+def run_rough_block(args):
+    """2048 x 2048 discs on a Gaussian height field with a per-disc sticking
+    field, 1e8 rays: forward trace and the adjoint dL/ds_j of the bottom-quarter
+    flux (held estimator), both timed with CUDA events."""
+    import torch
+
+    from rti_gb300 import Engine, scenes
+    from rti_gb300 import _lib as L
+    r = scenes.rough_discs(n=2048, spacing=0.01, rms=0.05, corr=0.2, seed=0)
+    rng = np.random.default_rng(1)
+    field = (1.0 / (1.0 + np.exp(-rng.normal(-2.0, 0.5, r.n)))).astype(np.float32)
+    dev = torch.device("cuda", 0)
+    rays = args.rough_rays
+    with Engine(0) as e:
+        e.set_tree_builder(L.RTG_TREE_PLOC)
+        t0 = time.perf_counter()
+        e.upload_discs(r.points, r.normals, r.radii)
+        build_s = time.perf_counter() - t0
+        e.configure(box=(r.box_lo, r.box_hi), x_bound=1, y_bound=1, reset=True)
+        cs = torch.cuda.current_stream(dev).cuda_stream  # the events below are recorded on this stream
+        f_dev = torch.from_numpy(field).to(dev)
+        e.set_sticking_field_device(f_dev.data_ptr(), r.n, cs)
+        z = r.points[:, 2]
+        g = torch.from_numpy((z < np.quantile(z, 0.25)).astype(np.float64)).to(dev)
+        fg = torch.zeros(r.n, dtype=torch.float64, device=dev)
+        sc = torch.zeros(2, dtype=torch.float64, device=dev)
+
+        def timed(fn, reps=2):
+            out = []
+            for k in range(reps + 1):
+                a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a0.record()
+                fn(k)
+                a1.record()
+                torch.cuda.synchronize()
+                if k > 0:
+                    out.append(a0.elapsed_time(a1))
+            return statistics.mean(out)
+
+        fwd_ms = timed(lambda k: e.trace(rays, seed=k, stream=cs))
+        t = e.tally()
+        adj_ms = timed(lambda k: e.adjoint_device(g.data_ptr(), 0, rays, k, fg.data_ptr(), sc.data_ptr(),
+                                                  unbiased=False, stream=cs))
+    return {"workload": "2048^2 discs on a Gaussian height field (rms 0.05, corr 0.2, spacing 0.01), per-disc "
+                        "sticking logistic(N(-2,0.5)), cosine source, x/y periodic; L = flux onto the lowest "
+                        "quarter of the discs",
+            "discs": int(r.n), "rays": rays, "tree": "PLOC", "build_s": build_s,
+            "forward_ms": fwd_ms, "rays_per_s": rays / fwd_ms * 1e3, "segments": t.segments,
+            "adjoint_field_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+            "grad_evals_per_s": 1e3 / (fwd_ms + adj_ms), "errors": t.errors}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -401,6 +455,9 @@ def run_ours(args):
     batch = None
     if rank == 0 and world == 1 and not args.no_batch:
         batch = run_batch_block(args)
+    rough = None
+    if rank == 0 and world == 1 and not args.no_rough:
+        rough = run_rough_block(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -413,7 +470,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f64 accumulators",
                 "data": "synthetic", "config": config_dict(h, R), "clocks": clocks, "roofline": roof,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps, "adjoint": adj,
-                "plain_gpu": plain, "batch": batch,
+                "plain_gpu": plain, "batch": batch, "rough_field": rough,
                 "wall_s_timed_region": wall,
                 "tally_per_step": {"segments": seg, "hitc": statistics.mean(t.hitc for t in tallies),
                                    "truncated": max(t.truncated for t in tallies),
@@ -440,6 +497,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-rays", type=int, default=2_000_000, help="rays per job of the batch block")
+    ap.add_argument("--no-rough", action="store_true")
+    ap.add_argument("--rough-rays", type=int, default=100_000_000, help="rays of the rough-surface block")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     from __graft_entry__ import build

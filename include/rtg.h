@@ -165,11 +165,26 @@ RTG_API int rtg_set_launch_config(rtg_context* ctx, const rtg_launch_config* lc)
 RTG_API int rtg_get_launch_config(const rtg_context* ctx, rtg_launch_config* lc);
 /* Internal nodes on the longest root-to-leaf path of the context's LBVH. */
 RTG_API int rtg_get_tree_depth(const rtg_context* ctx, int32_t* depth);
-/* Autotuner: times each candidate launch configuration (block size x packet
- * x stack depth x scheduling) on source rays [0, sample_rays) with `seed`
- * under the current surface and configuration, keeps the fastest as the
- * context's launch configuration and returns it (best and best_rays_per_s
- * may be NULL).  Leaves no trace results behind (trace again afterwards). */
+/* Topology of the tree over the Morton-sorted primitives (no counterpart in
+ * rti, whose Embree build quality is fixed at HIGH, tracer.hpp:85):
+ *   RTG_TREE_KARRAS: radix tree split at the highest differing key bit
+ *     (Karras, HPG 2012); the fastest build; best on regular grids;
+ *   RTG_TREE_PLOC: locally-ordered clustering by merged surface area (Meister
+ *     and Bittner, TVCG 2018); 2-3x the build time, fewer node visits on
+ *     irregular surfaces.
+ * Setting it rebuilds the tree of the current geometry and applies to later
+ * uploads.  Results do not depend on it.  rtg_autotune tries both. */
+#define RTG_TREE_KARRAS 0
+#define RTG_TREE_PLOC 1
+RTG_API int rtg_set_tree_builder(rtg_context* ctx, int32_t builder);
+RTG_API int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder);
+/* Autotuner: for each tree builder (RTG_TREE_*), times each candidate launch
+ * configuration (block size x packet x stack depth x scheduling) on source
+ * rays [0, sample_rays) with `seed` under the current surface and
+ * configuration; keeps the fastest pair as the context's tree and launch
+ * configuration and returns the latter (best and best_rays_per_s may be NULL;
+ * rtg_get_tree_builder tells the tree).  Leaves no trace results behind
+ * (trace again afterwards). */
 RTG_API int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
                          double* best_rays_per_s);
 

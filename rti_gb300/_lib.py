@@ -43,7 +43,7 @@ EXPORTS = [
     "rtg_batch_get_tally", "rtg_launch_config_default", "rtg_set_launch_config", "rtg_get_launch_config",
     "rtg_get_tree_depth", "rtg_autotune", "rtg_batch_set_launch_config", "rtg_batch_get_launch_config",
     "rtg_batch_autotune", "rtg_write_vtp", "rtg_write_vtp_discs", "rtg_write_vtp_triangles", "rtg_write_vtp_mixed",
-    "rtg_read_point_cloud", "rtg_read_triangles",
+    "rtg_read_point_cloud", "rtg_read_triangles", "rtg_set_tree_builder", "rtg_get_tree_builder",
 ]
 
 RTG_ADJ_HELD = 0
@@ -51,6 +51,8 @@ RTG_ADJ_UNBIASED = 1
 RTG_SCHED_MEGAKERNEL = 0
 RTG_SCHED_WAVEFRONT = 1
 RTG_SCHED_PLAIN = 2
+RTG_TREE_KARRAS = 0
+RTG_TREE_PLOC = 1
 
 
 class RtgConfig(C.Structure):
@@ -184,6 +186,8 @@ def load(path: str | None = None):
                                           C.POINTER(C.c_char_p), C.c_int32]),
         "rtg_read_point_cloud": (C.c_int, [C.c_char_p, _i64p, _f32p, _f32p, _f32p, C.c_char_p, C.c_int32]),
         "rtg_read_triangles": (C.c_int, [C.c_char_p, _i64p, _f32p, _i64p, _u32p, C.c_char_p, C.c_int32]),
+        "rtg_set_tree_builder": (C.c_int, [_ctx, C.c_int32]),
+        "rtg_get_tree_builder": (C.c_int, [_ctx, _i32p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

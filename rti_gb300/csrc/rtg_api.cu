@@ -497,6 +497,29 @@ int rtg_get_tree_depth(const rtg_context* ctx, int32_t* depth) {
   return RTG_OK;
 }
 
+int rtg_set_tree_builder(rtg_context* ctx, int32_t builder) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (builder != RTG_TREE_KARRAS && builder != RTG_TREE_PLOC)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "builder must be RTG_TREE_KARRAS or RTG_TREE_PLOC");
+  RTG_TRY(use_device(ctx));
+  const int32_t keep = ctx->g.builder;
+  ctx->g.builder = builder;
+  if (ctx->g.nd + ctx->g.nt > 0 && ctx->g.nodes.p && builder != keep) {
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int rc = build_lbvh(ctx);
+    if (rc != RTG_OK) return rc;
+    ctx->traced = false;
+    ctx->finalized = false;
+  }
+  return RTG_OK;
+}
+
+int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder) {
+  if (!ctx || !builder) return RTG_ERR_INVALID_ARGUMENT;
+  *builder = ctx->g.builder;
+  return RTG_OK;
+}
+
 int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
                  double* best_rays_per_s) {
   if (!ctx || sample_rays == 0) return RTG_ERR_INVALID_ARGUMENT;
@@ -505,6 +528,7 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
   const int64_t np = ctx->g.nd + ctx->g.nt;
   cudaStream_t st = ctx->stream;
   const rtg_launch_config keep = ctx->lc;
+  const int32_t keep_builder = ctx->g.builder;
   auto run = [&](const rtg_launch_config& lc, float& ms) -> int {
     ctx->lc = lc;
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * np * sizeof(double), st));
@@ -517,44 +541,57 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
     RTG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->evk0, ctx->evk1));
     return RTG_OK;
   };
-  std::vector<rtg_launch_config> cand;
-  for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT, RTG_SCHED_PLAIN})
-    for (int tpb : {64, 128, 256})
-      for (int packet : {1, 8, 32})
-        for (int stack : {0, 256}) {
-          if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
-          if (sched == RTG_SCHED_WAVEFRONT && (packet != 1 || tpb == 64)) continue;  // no refill in a wavefront
-          if (stack == 256 && stack_for(0, ctx->g.depth) == 256) continue;
-          cand.push_back(rtg_launch_config{tpb, packet, stack, sched});
-        }
-  std::vector<float> best_ms(cand.size(), 0.0f);
+  struct Cand {
+    int32_t builder;
+    rtg_launch_config lc;
+    float ms;
+  };
+  std::vector<Cand> cand;
   int rc = RTG_OK;
-  float ms = 0.0f;
-  for (size_t i = 0; i < cand.size() && rc == RTG_OK; ++i) {
-    rc = run(cand[i], ms);  // warm-up (and, for the wavefront, its queue allocation)
-    if (rc == RTG_OK) rc = run(cand[i], best_ms[i]);
-  }
-  // the three fastest again, keep each one's best time
-  std::vector<size_t> order(cand.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return best_ms[a] < best_ms[b]; });
-  for (size_t r = 0; r < 2 && rc == RTG_OK; ++r)
-    for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
-      rc = run(cand[order[q]], ms);
-      if (rc == RTG_OK && ms < best_ms[order[q]]) best_ms[order[q]] = ms;
+  for (int32_t builder : {RTG_TREE_KARRAS, RTG_TREE_PLOC}) {
+    if (rc != RTG_OK) break;
+    rc = rtg_set_tree_builder(ctx, builder);
+    if (rc == RTG_OK) rc = prepare_trace(ctx, 0, sample_rays, seed, p);  // the tree changed
+    if (rc != RTG_OK) break;
+    const size_t first = cand.size();
+    for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT, RTG_SCHED_PLAIN})
+      for (int tpb : {64, 128, 256})
+        for (int packet : {1, 8, 32})
+          for (int stack : {0, 256}) {
+            if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
+            if (sched == RTG_SCHED_WAVEFRONT && (packet != 1 || tpb == 64)) continue;  // no refill in a wavefront
+            if (stack == 256 && stack_for(0, ctx->g.depth) == 256) continue;
+            cand.push_back(Cand{builder, rtg_launch_config{tpb, packet, stack, sched}, 0.0f});
+          }
+    float ms = 0.0f;
+    for (size_t i = first; i < cand.size() && rc == RTG_OK; ++i) {
+      rc = run(cand[i].lc, ms);  // warm-up (and, for the wavefront, its queue allocation)
+      if (rc == RTG_OK) rc = run(cand[i].lc, cand[i].ms);
     }
+    // the three fastest of this tree again, keep each one's best time
+    std::vector<size_t> order;
+    for (size_t i = first; i < cand.size(); ++i) order.push_back(i);
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cand[a].ms < cand[b].ms; });
+    for (size_t r = 0; r < 2 && rc == RTG_OK; ++r)
+      for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
+        rc = run(cand[order[q]].lc, ms);
+        if (rc == RTG_OK && ms < cand[order[q]].ms) cand[order[q]].ms = ms;
+      }
+  }
   ctx->traced = false;
   ctx->finalized = false;
-  if (rc != RTG_OK) {
+  if (rc != RTG_OK || cand.empty()) {
     ctx->lc = keep;
-    return rc;
+    rtg_set_tree_builder(ctx, keep_builder);
+    return rc != RTG_OK ? rc : set_error(ctx, RTG_ERR_INTERNAL, "autotune found no candidate");
   }
   size_t bi = 0;
   for (size_t i = 1; i < cand.size(); ++i)
-    if (best_ms[i] < best_ms[bi]) bi = i;
-  ctx->lc = cand[bi];
-  if (best) *best = cand[bi];
-  if (best_rays_per_s) *best_rays_per_s = best_ms[bi] > 0.0f ? sample_rays / (best_ms[bi] * 1e-3) : 0.0;
+    if (cand[i].ms < cand[bi].ms) bi = i;
+  RTG_TRY(rtg_set_tree_builder(ctx, cand[bi].builder));
+  ctx->lc = cand[bi].lc;
+  if (best) *best = cand[bi].lc;
+  if (best_rays_per_s) *best_rays_per_s = cand[bi].ms > 0.0f ? sample_rays / (cand[bi].ms * 1e-3) : 0.0;
   return RTG_OK;
 }
 

@@ -26,6 +26,10 @@ struct __align__(16) Node {
   uint4 d;
 };
 
+// LBVH topology builders over the Morton-ordered leaves.
+constexpr int32_t kBuilderKarras = 0;  // Karras 2012 radix tree (split at the highest differing key bit)
+constexpr int32_t kBuilderPloc = 1;    // Meister and Bittner 2018 locally-ordered clustering
+
 // Device status counters (accumulated over a trace).
 struct DevTally {
   unsigned long long hitc, nonhitc, total, segments, truncated, nb_deposits, errors, next_ray;
@@ -123,6 +127,7 @@ struct Geometry {
   float rmax = 0.0f;
   float tri_min[3] = {0, 0, 0}, tri_max[3] = {0, 0, 0};
   int32_t depth = 0;  // internal nodes on the longest root-to-leaf path
+  int32_t builder = 0;  // kBuilderKarras or kBuilderPloc
 };
 
 // Wavefront scheduling state (device buffers, lazily allocated).

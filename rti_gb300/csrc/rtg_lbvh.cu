@@ -9,6 +9,8 @@
 //   5. primitives copied to slot order (LBVH leaf order) for coherent access,
 //   6. bottom-up box refit with per-node arrival counters.
 // rtg_update_* reruns 1, 5 and 6 only (moved surface, same topology).
+// Step 4 is by default replaced by PLOC clustering over the same sorted
+// leaves (build_ploc), whose trees need fewer node visits per query.
 //
 // Leaves hold one primitive; each internal node stores the boxes of both
 // children (64 bytes), so one node fetch decides both children.
@@ -192,6 +194,148 @@ __global__ void karras_kernel(const uint32_t* __restrict__ m, int64_t n, const u
   nodes[i].d = make_uint4(left, right, 0u, 0u);
 }
 
+
+// ---- PLOC: parallel locally-ordered clustering (Meister and Bittner, TVCG
+// 2018), an agglomerative build over the Morton-ordered leaves.  Each round,
+// every cluster finds the neighbour within kPlocRadius positions whose merged
+// box has the smallest surface area (ties: the lower position); mutual pairs
+// merge into a new internal node; the survivors are compacted in order.
+// Node indices are handed out from the top down, round by round and in
+// position order, so the root is node 0 and the layout is deterministic.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocThreads = 256;
+constexpr uint32_t kClusterLeaf = 0x80000000u;  // cluster = sorted leaf index | bit 31, else a node index
+
+__global__ void ploc_init_kernel(const uint32_t* __restrict__ sorted_prim, int64_t n, const float* __restrict__ plo,
+                                 const float* __restrict__ phi, uint32_t* __restrict__ cid, float4* __restrict__ blo,
+                                 float4* __restrict__ bhi) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t p = sorted_prim[i];
+  cid[i] = kClusterLeaf | (uint32_t)i;
+  blo[i] = make_float4(plo[3 * p], plo[3 * p + 1], plo[3 * p + 2], 0.0f);
+  bhi[i] = make_float4(phi[3 * p], phi[3 * p + 1], phi[3 * p + 2], 0.0f);
+}
+
+__device__ __forceinline__ float merged_area(float4 al, float4 ah, float4 bl, float4 bh) {
+  const float dx = fmaxf(ah.x, bh.x) - fminf(al.x, bl.x);
+  const float dy = fmaxf(ah.y, bh.y) - fminf(al.y, bl.y);
+  const float dz = fmaxf(ah.z, bh.z) - fminf(al.z, bl.z);
+  return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void __launch_bounds__(kPlocThreads) ploc_nn_kernel(const float4* __restrict__ blo,
+                                                               const float4* __restrict__ bhi,
+                                                               const uint64_t* __restrict__ state,
+                                                               uint32_t* __restrict__ nn) {
+  __shared__ float4 slo[kPlocThreads + 2 * kPlocRadius], shi[kPlocThreads + 2 * kPlocRadius];
+  const int64_t n = (int64_t)state[0];
+  if (n < 2 || (int64_t)blockIdx.x * kPlocThreads >= n) return;
+  const int64_t b0 = (int64_t)blockIdx.x * kPlocThreads;
+  for (int k = threadIdx.x; k < kPlocThreads + 2 * kPlocRadius; k += kPlocThreads) {
+    const int64_t j = b0 - kPlocRadius + k;
+    if (j >= 0 && j < n) {
+      slo[k] = blo[j];
+      shi[k] = bhi[j];
+    }
+  }
+  __syncthreads();
+  const int64_t i = b0 + threadIdx.x;
+  if (i >= n) return;
+  const int li = threadIdx.x + kPlocRadius;
+  const float4 al = slo[li], ah = shi[li];
+  float best = INFINITY;
+  int64_t bj = i > 0 ? i - 1 : i + 1;
+  for (int d = -kPlocRadius; d <= kPlocRadius; ++d) {
+    const int64_t j = i + d;
+    if (d == 0 || j < 0 || j >= n) continue;
+    const float a = merged_area(al, ah, slo[li + d], shi[li + d]);
+    if (a < best) {
+      best = a;
+      bj = j;
+    }
+  }
+  nn[i] = (uint32_t)bj;
+}
+
+// Per position: (survives << 32) | merges-with-its-higher-mutual-neighbour,
+// zero beyond the current cluster count (the scan length is an upper bound).
+// The higher member of a mutual pair is absorbed.
+__global__ void ploc_flags_kernel(const uint32_t* __restrict__ nn, int64_t bound, const uint64_t* __restrict__ state,
+                                  unsigned long long* __restrict__ packed) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= bound) return;
+  const int64_t n = (int64_t)state[0];
+  if (i >= n) {
+    packed[i] = 0ull;
+    return;
+  }
+  if (n < 2) {
+    packed[i] = 1ull << 32;
+    return;
+  }
+  const uint32_t j = nn[i];
+  const bool mutual = nn[j] == (uint32_t)i;
+  const unsigned long long merge = (mutual && (uint32_t)i < j) ? 1ull : 0ull;
+  const unsigned long long keep = (mutual && (uint32_t)i > j) ? 0ull : 1ull;
+  packed[i] = (keep << 32) | merge;
+}
+
+// After the scan: state[0] = surviving clusters, state[1] += merges; a round
+// without a merge while clusters remain is recorded in state[2].
+__global__ void ploc_update_kernel(const unsigned long long* __restrict__ total, uint64_t* __restrict__ state) {
+  const unsigned long long t = *total;
+  const uint64_t merges = t & 0xFFFFFFFFull, kept = t >> 32;
+  if (merges == 0 && state[0] > 1) state[2] = 1;
+  state[0] = kept;
+  state[1] += merges;
+}
+
+__global__ void ploc_merge_kernel(const uint32_t* __restrict__ nn, int64_t bound,
+                                  const uint64_t* __restrict__ state, const uint32_t* __restrict__ cid,
+                                  const float4* __restrict__ blo, const float4* __restrict__ bhi,
+                                  const unsigned long long* __restrict__ packed, uint32_t n_int,
+                                  const uint32_t* __restrict__ leaf_ref, int64_t nleaves, Node* __restrict__ nodes,
+                                  uint32_t* __restrict__ parent, uint32_t* __restrict__ cid_out,
+                                  float4* __restrict__ blo_out, float4* __restrict__ bhi_out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n = (int64_t)state[0];
+  if (i >= bound || i >= n) return;
+  if (n < 2) {  // the finished root cluster: carried over unchanged
+    cid_out[0] = cid[0];
+    blo_out[0] = blo[0];
+    bhi_out[0] = bhi[0];
+    return;
+  }
+  const uint32_t j = nn[i];
+  const bool mutual = nn[j] == (uint32_t)i;
+  if (mutual && (uint32_t)i > j) return;  // absorbed by j
+  // positions after compaction (high word) and merge ranks (low word) come
+  // from the exclusive scan; nodes are handed out downwards from node_top
+  const uint32_t pos = (uint32_t)(packed[i] >> 32);
+  const uint32_t rank = (uint32_t)(packed[i] & 0xFFFFFFFFull);
+  const uint32_t node_top = n_int - 1u - (uint32_t)state[1];
+  if (mutual) {
+    const uint32_t idx = node_top - rank;
+    const uint32_t a = cid[i], b = cid[j];
+    const uint32_t ra = (a & kClusterLeaf) ? leaf_ref[a & ~kClusterLeaf] : a;
+    const uint32_t rb = (b & kClusterLeaf) ? leaf_ref[b & ~kClusterLeaf] : b;
+    nodes[idx].d = make_uint4(ra, rb, 0u, 0u);
+    if (a & kClusterLeaf) parent[(nleaves - 1) + (a & ~kClusterLeaf)] = idx;
+    else parent[a] = idx;
+    if (b & kClusterLeaf) parent[(nleaves - 1) + (b & ~kClusterLeaf)] = idx;
+    else parent[b] = idx;
+    const float4 al = blo[i], ah = bhi[i], bl = blo[j], bh = bhi[j];
+    cid_out[pos] = idx;
+    blo_out[pos] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.0f);
+    bhi_out[pos] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f);
+  } else {
+    cid_out[pos] = cid[i];
+    blo_out[pos] = blo[i];
+    bhi_out[pos] = bhi[i];
+  }
+}
+
 __device__ __forceinline__ void child_box(uint32_t ref, const float4* __restrict__ dn,
                                           const float4* __restrict__ tri, const float* __restrict__ plo,
                                           const float* __restrict__ phi, const float* node_box, float* lo,
@@ -370,6 +514,87 @@ int validate_tree(rtg_context* ctx, cudaStream_t st) {
   return RTG_OK;
 }
 
+
+// Binary tree over the np sorted leaves by PLOC (see ploc_* kernels): writes
+// the child references of nodes [0, np-1) and the parent array; boxes come
+// from the refit that follows.
+int build_ploc(rtg_context* ctx, const uint32_t* d_sorted_prim, cudaStream_t st) {
+  Geometry& g = ctx->g;
+  const int64_t n = g.nd + g.nt;
+  DBuf<uint32_t> cid[2], nn;
+  DBuf<float4> blo[2], bhi[2];
+  DBuf<int64_t> packed, total;
+  DBuf<uint64_t> state;  // [0] clusters, [1] nodes allocated, [2] stall flag
+  auto cleanup = [&]() {
+    for (int q = 0; q < 2; ++q) {
+      dfree(cid[q]);
+      dfree(blo[q]);
+      dfree(bhi[q]);
+    }
+    dfree(nn);
+    dfree(packed);
+    dfree(total);
+    dfree(state);
+  };
+  int rc = RTG_OK;
+  for (int q = 0; q < 2 && rc == RTG_OK; ++q) {
+    rc = dalloc(ctx, cid[q], (size_t)n, "PLOC clusters");
+    if (rc == RTG_OK) rc = dalloc(ctx, blo[q], (size_t)n, "PLOC boxes");
+    if (rc == RTG_OK) rc = dalloc(ctx, bhi[q], (size_t)n, "PLOC boxes");
+  }
+  if (rc == RTG_OK) rc = dalloc(ctx, nn, (size_t)n, "PLOC neighbours");
+  if (rc == RTG_OK) rc = dalloc(ctx, packed, (size_t)n, "PLOC scan");
+  if (rc == RTG_OK) rc = dalloc(ctx, total, 1, "PLOC totals");
+  if (rc == RTG_OK) rc = dalloc(ctx, state, 3, "PLOC state");
+  if (rc != RTG_OK) {
+    cleanup();
+    return rc;
+  }
+  const uint64_t init[3] = {(uint64_t)n, 0, 0};
+  cudaMemcpyAsync(state.p, init, sizeof init, cudaMemcpyHostToDevice, st);
+  ploc_init_kernel<<<blocks_for(n, 256), 256, 0, st>>>(d_sorted_prim, n, g.prim_lo.p, g.prim_hi.p, cid[0].p,
+                                                        blo[0].p, bhi[0].p);
+  const uint32_t n_int = (uint32_t)(n - 1);
+  int64_t bound = n;  // the cluster count is only read back between chunks of rounds
+  int q = 0;
+  uint64_t h[3] = {(uint64_t)n, 0, 0};
+  for (int chunk = 0; h[0] > 1; ++chunk) {
+    if (chunk > 10000) {
+      rc = set_error(ctx, RTG_ERR_INTERNAL, "PLOC did not converge");
+      break;
+    }
+    for (int r = 0; r < 4 && rc == RTG_OK; ++r) {
+      const unsigned nb = (unsigned)((bound + kPlocThreads - 1) / kPlocThreads);
+      ploc_nn_kernel<<<nb, kPlocThreads, 0, st>>>(blo[q].p, bhi[q].p, state.p, nn.p);
+      ploc_flags_kernel<<<blocks_for(bound, 256), 256, 0, st>>>(nn.p, bound, state.p,
+                                                                (unsigned long long*)packed.p);
+      rc = exclusive_scan_i64(ctx, packed.p, bound, total.p, st);
+      ploc_merge_kernel<<<blocks_for(bound, 256), 256, 0, st>>>(
+          nn.p, bound, state.p, cid[q].p, blo[q].p, bhi[q].p, (const unsigned long long*)packed.p, n_int,
+          g.leaf_ref.p, n, g.nodes.p, g.parent.p, cid[q ^ 1].p, blo[q ^ 1].p, bhi[q ^ 1].p);
+      ploc_update_kernel<<<1, 1, 0, st>>>((const unsigned long long*)total.p, state.p);
+      q ^= 1;
+    }
+    if (rc != RTG_OK) break;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, state.p, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      rc = check_cuda(ctx, e, "PLOC round");
+      break;
+    }
+    if (h[2] != 0 || h[1] > n_int) {
+      rc = set_error(ctx, RTG_ERR_INTERNAL, "PLOC round without progress");
+      break;
+    }
+    bound = (int64_t)h[0];
+  }
+  if (rc == RTG_OK && h[1] != n_int) rc = set_error(ctx, RTG_ERR_INTERNAL, "PLOC node count mismatch");
+  cudaStreamSynchronize(st);
+  cleanup();
+  return rc;
+}
+
 int run_bounds(rtg_context* ctx, uint32_t* d_cbounds, cudaStream_t st) {
   Geometry& g = ctx->g;
   const int64_t np = g.nd + g.nt;
@@ -466,10 +691,22 @@ int build_lbvh(rtg_context* ctx) {
                                                       g.leaf_prim.p);
     if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "slots"); break; }
     if (np > 1) {
-      cudaMemsetAsync(g.parent.p, 0xFF, 2 * np * sizeof(uint32_t), st);
-      karras_kernel<<<blocks_for(np - 1, 256), 256, 0, st>>>(keys.p, np, g.leaf_ref.p, g.nodes.p, g.parent.p);
-      if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "karras"); break; }
-      if ((rc = validate_tree(ctx, st)) != RTG_OK) break;
+      // PLOC first; a clustering deeper than the traversal stacks allow (possible
+      // for degenerate inputs) falls back to the Karras tree, whose depth is
+      // bounded by the key length
+      bool karras = g.builder != kBuilderPloc;
+      if (!karras) {
+        cudaMemsetAsync(g.parent.p, 0xFF, 2 * np * sizeof(uint32_t), st);
+        if ((rc = build_ploc(ctx, vals.p, st)) != RTG_OK) break;
+        if ((rc = validate_tree(ctx, st)) != RTG_OK) break;
+        karras = tree_depth(ctx, st) != RTG_OK;
+      }
+      if (karras) {
+        cudaMemsetAsync(g.parent.p, 0xFF, 2 * np * sizeof(uint32_t), st);
+        karras_kernel<<<blocks_for(np - 1, 256), 256, 0, st>>>(keys.p, np, g.leaf_ref.p, g.nodes.p, g.parent.p);
+        if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "karras"); break; }
+        if ((rc = validate_tree(ctx, st)) != RTG_OK) break;
+      }
     }
     if ((rc = tree_depth(ctx, st)) != RTG_OK) break;
     rc = run_slots_and_refit(ctx, nullptr, nullptr, st);

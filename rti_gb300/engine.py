@@ -174,6 +174,16 @@ class Engine:
         self._check(self._L.rtg_get_tree_depth(self._h, C.byref(d)))
         return d.value
 
+    @property
+    def tree_builder(self) -> int:
+        b = C.c_int32()
+        self._check(self._L.rtg_get_tree_builder(self._h, C.byref(b)))
+        return b.value
+
+    def set_tree_builder(self, builder: int):
+        """L.RTG_TREE_KARRAS (fast build) or L.RTG_TREE_PLOC (clustering); rebuilds the current tree."""
+        self._check(self._L.rtg_set_tree_builder(self._h, int(builder)))
+
     def autotune(self, sample_rays: int, seed: int = 0):
         """Times the candidate launch configurations on a sample trace and keeps
         the fastest; returns (config dict, rays/s of the sample)."""

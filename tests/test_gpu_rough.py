@@ -32,6 +32,7 @@ def test_rough_surface_field_gradient_spot_checks(rtg_lib):
     field = (1.0 / (1.0 + np.exp(-rng.normal(-2.0, 0.5, r.n)))).astype(np.float32)
     dev = torch.device("cuda", 0)
     with Engine(0) as e:
+        e.set_tree_builder(1)  # clustered tree: about 30 % fewer node visits than the radix tree here
         t0 = time.perf_counter()
         e.upload_discs(r.points, r.normals, r.radii)
         build_s = time.perf_counter() - t0

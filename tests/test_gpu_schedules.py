@@ -61,6 +61,14 @@ def test_every_launch_config_gives_the_same_trace(eng, scene):
         eng.set_launch_config(*cfg)
         _same(ref, _run(eng, 60000, 4))
     eng.set_launch_config()
+    # the clustered tree (PLOC) instead of the radix tree: same hits
+    eng.set_tree_builder(1)
+    assert eng.tree_builder == 1 and 1 <= eng.tree_depth <= 256
+    _same(ref, _run(eng, 60000, 4))
+    eng.set_launch_config(256, 8, 0, MK)
+    _same(ref, _run(eng, 60000, 4))
+    eng.set_tree_builder(0)
+    eng.set_launch_config()
 
 
 def test_wavefront_truncation_field_and_reflective_box(eng):
@@ -93,9 +101,10 @@ def test_autotune_picks_a_valid_config_and_results_stay(eng):
     cfg, rate = eng.autotune(80000, seed=1)
     assert rate > 0
     assert cfg["threads_per_block"] in (64, 128, 256) and 1 <= cfg["packet"] <= 32
-    assert eng.launch_config().as_dict() == cfg
+    assert eng.launch_config().as_dict() == cfg and eng.tree_builder in (0, 1)
     _same(ref, _run(eng, 80000, 1))
     eng.set_launch_config()
+    eng.set_tree_builder(0)
 
 
 def test_batch_wavefront_and_autotune(rtg_lib):
