@@ -11,19 +11,23 @@
 // Differences a caller can see:
 //   * no Embree and no VTK: RTCRay / RTCHit below are plain structs with
 //     Embree's field names so that existing particle classes compile;
-//   * the particle's get_sticking_probability() is called once per disc on
-//     the host (normal-incidence ray, hit.primID = disc id) and the results
-//     go to the GPU as a sticking field, so a sticking that depends on the
-//     incoming direction or on random state is evaluated at normal incidence;
-//   * reflection_type selects diffuse or specular re-emission
-//     (rti::reflection::diffuse / specular below, or any type providing
+//   * sticking comes from the particle type: `static constexpr rtg_sticking`
+//     (one value), else a member get_sticking_field() (one value per disc),
+//     else get_sticking_probability() called once per disc on the host
+//     (normal-incidence ray, hit.primID = disc id) -- so a sticking that
+//     depends on the incoming direction or on random state is evaluated at
+//     normal incidence;
+//   * reflection_type selects diffuse, specular or mixed re-emission
+//     (rti::reflection::diffuse / specular / mixed below, or any type providing
 //     `static constexpr int rtg_mode` and `static constexpr float
 //     rtg_specular_fraction`);
 //   * set(direction) takes effect (cosine_direction_z or
 //     power_cosine_direction_z); in the reference it leaves the cosine source
 //     in place (device.hpp:77-80, 295-296);
 //   * errors throw std::runtime_error with librtg's message, where the
-//     reference asserts.
+//     reference asserts;
+//   * extra getters: get_values() (raw S1 per disc, FP64), get_relative_error(),
+//     get_vov().
 #pragma once
 
 #include <array>
@@ -134,6 +138,16 @@ class specular : public i_reflection<Ty> {
   static constexpr int rtg_mode = RTG_REFLECT_SPECULAR;
   static constexpr float rtg_specular_fraction = 1.0f;
 };
+// Specular with probability SpecularPercent / 100, else diffuse (no
+// counterpart in rti; the mixture of the hole benchmark).
+template <typename Ty, int SpecularPercent>
+class mixed : public i_reflection<Ty> {
+  static_assert(0 <= SpecularPercent && SpecularPercent <= 100, "a percentage");
+
+ public:
+  static constexpr int rtg_mode = RTG_REFLECT_MIXED;
+  static constexpr float rtg_specular_fraction = SpecularPercent / 100.0f;
+};
 }  // namespace reflection
 
 namespace ray {
@@ -158,6 +172,19 @@ class power_cosine_direction_z : public i_direction<Ty> {  // ray/power_cosine_d
   Ty exp_;
 };
 }  // namespace ray
+
+namespace detail {
+// particle_type::get_sticking_field() -> one sticking value per disc
+template <typename P, typename = void>
+struct has_sticking_field : std::false_type {};
+template <typename P>
+struct has_sticking_field<P, std::void_t<decltype(std::declval<P&>().get_sticking_field())>> : std::true_type {};
+// particle_type::rtg_sticking -> one constant sticking for every disc
+template <typename P, typename = void>
+struct has_constant_sticking : std::false_type {};
+template <typename P>
+struct has_constant_sticking<P, std::void_t<decltype(P::rtg_sticking)>> : std::true_type {};
+}  // namespace detail
 
 using ::rti::geo::bound_condition;
 using ::rti::particle::i_particle;
@@ -187,7 +214,6 @@ class device final {
     if (points.size() != spacing.size() || points.size() != normals.size())
       throw std::runtime_error("rti::device: points, normals and grid spacing differ in length");
     const size_t n = points.size();
-    std::vector<float> sticking = sticking_per_disc();
     rtg_config cfg;
     rtg_config_default(&cfg);
     cfg.x_bound = xCond == bound_condition::PERIODIC ? RTG_BOUND_PERIODIC : RTG_BOUND_REFLECTIVE;
@@ -195,16 +221,39 @@ class device final {
     cfg.reflection = reflection_type::rtg_mode;
     cfg.specular_fraction = reflection_type::rtg_specular_fraction;
     cfg.source_exponent = (float)exponent;
+    std::vector<float> field;
+    if constexpr (detail::has_constant_sticking<particle_type>::value) {
+      cfg.sticking = (float)particle_type::rtg_sticking;
+    } else {
+      field = sticking_per_disc();
+    }
+    rtg_context* raw = nullptr;
+    check(rtg_create(&raw, cuda_device), nullptr, "no usable CUDA device");
+    std::unique_ptr<rtg_context, int (*)(rtg_context*)> ctx(raw, rtg_destroy);
+    check(rtg_upload_discs(raw, &points[0][0], &normals[0][0], spacing.data(), (int64_t)n), raw, "upload");
+    check(rtg_set_config(raw, &cfg), raw, "configuration");
+    if (!field.empty()) check(rtg_set_sticking_field(raw, field.data(), (int64_t)n), raw, "sticking");
+    check(rtg_trace(raw, (uint64_t)numofrays, seed, nullptr), raw, "trace");
     mcestimates.assign(n, 0.0f);
     std::vector<uint64_t> cnt(n, 0);
-    int rc = rtg_device_run(&points[0][0], &normals[0][0], spacing.data(), (int64_t)n, &cfg, sticking.data(),
-                            (uint64_t)numofrays, seed, mcestimates.data(), cnt.data(), cuda_device);
-    if (rc != RTG_OK) throw std::runtime_error("rti::device::run failed with rtg status " + std::to_string(rc));
+    values.assign(n, 0.0);
+    relerr.assign(n, 0.0);
+    vov.assign(n, 0.0);
+    check(rtg_get_mc_estimates(raw, mcestimates.data()), raw, "estimates");
+    check(rtg_get_hit_counts(raw, cnt.data()), raw, "hit counts");
+    check(rtg_get_accumulators(raw, values.data(), nullptr, nullptr, nullptr), raw, "values");
+    check(rtg_get_relative_error(raw, relerr.data()), raw, "relative error");
+    check(rtg_get_vov(raw, vov.data()), raw, "variance of variance");
     hitcnts.assign(cnt.begin(), cnt.end());
   }
 
   std::vector<numeric_type> get_mc_estimates() { return mcestimates; }
   std::vector<size_t> get_hit_cnts() { return hitcnts; }
+  // Beyond rti's device (its hit accumulator's getters, hit_accumulator.hpp:
+  // 140-249): the raw flux S1 per disc in FP64, its relative error and VOV.
+  std::vector<double> get_values() { return values; }
+  std::vector<double> get_relative_error() { return relerr; }
+  std::vector<double> get_vov() { return vov; }
 
  private:
   struct disc_geometry : geo::meta_geometry<numeric_type> {
@@ -212,7 +261,20 @@ class device final {
     util::triple<numeric_type> get_normal(unsigned int id) override { return (*nrm)[id]; }
   };
 
+  static void check(int rc, rtg_context* ctx, const char* what) {
+    if (rc != RTG_OK)
+      throw std::runtime_error(std::string("rti::device: ") + what + ": " + (ctx ? rtg_last_error(ctx) : "") +
+                               " (rtg status " + std::to_string(rc) + ")");
+  }
+
   std::vector<float> sticking_per_disc() {
+    if constexpr (detail::has_sticking_field<particle_type>::value) {
+      particle_type particle{};
+      const auto f = particle.get_sticking_field();
+      if (f.size() != points.size())
+        throw std::runtime_error("rti::device: get_sticking_field() needs one value per disc");
+      return std::vector<float>(f.begin(), f.end());
+    }
     disc_geometry geo;
     geo.nrm = &normals;
     rng::splitmix_rng rng;
@@ -248,6 +310,7 @@ class device final {
   std::vector<numeric_type> spacing;
   std::vector<numeric_type> mcestimates;
   std::vector<size_t> hitcnts;
+  std::vector<double> values, relerr, vov;
   size_t numofrays = 1024;
   bound_condition xCond = bound_condition::REFLECTIVE;
   bound_condition yCond = bound_condition::REFLECTIVE;
