@@ -72,16 +72,40 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
-def read_traffic():
-    """Per-launch DRAM bytes of the path kernel from the committed ncu summary, or None."""
+def read_profile_line(key):
+    """A per-launch byte count of the path kernel from the committed ncu summary, or None."""
     p = os.path.join(ROOT, "profiles", "trace_paths_hole.md")
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].strip().split()[0])
     except OSError:
         pass
     return None
+
+
+def read_traffic():
+    return read_profile_line("traffic_bytes_per_launch")
+
+
+def l2_copy_gbs(dev):
+    """Copy bandwidth of a buffer pair that stays in L2 (2 x 24 MiB), best of 5
+    runs of 50 copies, CUDA events on the current stream: read + write bytes."""
+    import torch
+    a = torch.empty(24 << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(50):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * a.numel() * 50 / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return best
 
 
 class ClockSampler:
@@ -380,6 +404,16 @@ def run_ours(args):
             "kernel_ms": kms, "segments_per_launch": seg, "alg_bytes_per_launch": alg_bytes,
             "bytes_per_segment_model": f"64 + 64*{levels} + 4*{prim_bytes} (+16 per deposit)"}
 
+    # the same launch against the L2 roof (the tree and triangles are L2-resident):
+    # L2 bytes from ncu (lts__t_sectors.sum x 32 of a full-size launch) over the
+    # kernel's event time, against a measured L2-resident copy
+    l2_bytes = read_profile_line("l2_bytes_per_launch")
+    l2_peak = l2_copy_gbs(dev)
+    roof_l2 = {"bound": "l2", "peak": l2_peak, "peak_source": "measured here: 2 x 24 MiB device copy",
+               "unit": "GB/s", "traffic": l2_bytes,
+               "achieved": (l2_bytes / (kms / 1e3) / 1e9) if l2_bytes else None,
+               "frac": (l2_bytes / (kms / 1e3) / 1e9 / l2_peak) if l2_bytes else None}
+
     # end to end through the public API from host arrays
     e2e = None
     if not args.no_e2e:
@@ -469,6 +503,7 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f64 accumulators",
                 "data": "synthetic", "config": config_dict(h, R), "clocks": clocks, "roofline": roof,
+                "roofline_l2": roof_l2,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps, "adjoint": adj,
                 "plain_gpu": plain, "batch": batch, "rough_field": rough,
                 "wall_s_timed_region": wall,
