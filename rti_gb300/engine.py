@@ -273,7 +273,10 @@ class Engine:
         return s
 
     def values(self) -> np.ndarray:
-        return self.accumulators()[0]
+        """S1 (the flux per primitive, hit_accumulator::get_values) alone."""
+        out = np.zeros(self.num_primitives)
+        self._check(self._L.rtg_get_accumulators(self._h, _ptr(out, L._f64p), None, None, None))
+        return out
 
     def exposed_areas(self) -> np.ndarray:
         out = np.zeros(self.num_primitives, dtype=np.float32)
