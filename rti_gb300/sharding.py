@@ -5,7 +5,7 @@ id), so ranks trace disjoint ranges of ray ids against full replicas of the
 surface; the only exchange is the sum of the per-primitive accumulators
 (S1..S4, counts) and of the tallies, which reproduces tracer.hpp's OpenMP
 reduction of per-thread hit_accumulators (hit_accumulator.hpp:47-80) across
-processes.  On GPUs the accumulators are viewed in place (no copy) and summed
+processes -- and, for the adjoint, the sum of the gradients.  On GPUs the accumulators are viewed in place (no copy) and summed
 with NCCL; the same functions run on CPU tensors with gloo.
 """
 from __future__ import annotations
@@ -56,6 +56,18 @@ def allreduce_results(acc, cnt, tally: dict | None = None, group=None):
         for k, v in zip(keys, t.tolist()):
             tally[k] = v
     return acc, cnt, tally
+
+
+def allreduce_gradients(scalars, field_grad=None, group=None):
+    """Sums the adjoint's outputs over ranks in place: scalars = [dL/ds, dL/dn]
+    and, with a sticking field, dL/ds_j.  The replay of each rank's ray range
+    adds to its own buffers (rtg_adjoint accumulates), so the sum over ranks is
+    the gradient of the whole trace."""
+    import torch.distributed as dist
+    dist.all_reduce(scalars, group=group)
+    if field_grad is not None:
+        dist.all_reduce(field_grad, group=group)
+    return scalars, field_grad
 
 
 def stack_accumulators(s1, s2, s3, s4) -> np.ndarray:

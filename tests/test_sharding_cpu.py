@@ -9,7 +9,7 @@ import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
-from rti_gb300.sharding import allreduce_results, ray_range, stack_accumulators
+from rti_gb300.sharding import allreduce_gradients, allreduce_results, ray_range, stack_accumulators
 
 N_TOTAL = 6000
 
@@ -63,3 +63,42 @@ def test_two_gloo_ranks_equal_one_rank(tmp_path, oracle_lib):
     assert np.array_equal(cnt, ref.counts.astype(np.int64))
     np.testing.assert_allclose(acc, stack_accumulators(ref.s1, ref.s2, ref.s3, ref.s4), rtol=1e-12)
     assert list(tally) == [ref.hitc, ref.nonhitc, ref.segments, ref.total]
+
+
+def _adjoint_worker(rank, world, port, out_dir):
+    from oracle import oracle as O
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    s, cfg = _scene()
+    n = len(s.neighbors()[0]) - 1
+    g = np.linspace(0.0, 1.0, n)
+    field = np.linspace(0.05, 0.5, n).astype(np.float32)
+    b, e = ray_range(rank, world, N_TOTAL, scaling="strong")
+    ds, dn, fg, _ = O.adjoint(s, cfg, g, b, e, nthreads=1, sticking_field=field, unbiased=True)
+    sc = torch.tensor([ds, dn], dtype=torch.float64)
+    fgt = torch.from_numpy(np.asarray(fg, dtype=np.float64))
+    allreduce_gradients(sc, fgt)
+    if rank == 0:
+        np.save(os.path.join(out_dir, "sc.npy"), sc.numpy())
+        np.save(os.path.join(out_dir, "fg.npy"), fgt.numpy())
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_adjoint_equals_one_rank(tmp_path, oracle_lib):
+    """The adjoint of the sharded trace: per-rank replays of disjoint ray ranges
+    summed over two gloo ranks equal one replay of every ray."""
+    import socket
+    from oracle import oracle as O
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    mp.start_processes(_adjoint_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
+    s, cfg = _scene()
+    n = len(s.neighbors()[0]) - 1
+    g = np.linspace(0.0, 1.0, n)
+    field = np.linspace(0.05, 0.5, n).astype(np.float32)
+    ds, dn, fg, _ = O.adjoint(s, cfg, g, 0, N_TOTAL, nthreads=1, sticking_field=field, unbiased=True)
+    sc = np.load(tmp_path / "sc.npy")
+    np.testing.assert_allclose(sc, [ds, dn], rtol=1e-10)
+    np.testing.assert_allclose(np.load(tmp_path / "fg.npy"), fg, rtol=1e-10, atol=1e-12 * np.abs(fg).max())
