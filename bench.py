@@ -465,6 +465,18 @@ def run_ours(args):
                "adjoint_ms": adj_ms, "forward_ms": fwd_ms, "adjoint_over_forward": adj_ms / fwd_ms,
                "grad_evals_per_s": 1e3 / (fwd_ms + adj_ms), "rays_per_grad_eval": R}
 
+    # Monte Carlo error of the timed trace (hit_accumulator::get_relative_error
+    # per primitive): the metric is quoted at <= 1 % flux error, so report the
+    # error reached and the rays a 1 % median error needs (error ~ 1/sqrt(rays))
+    rel = eng.relative_error()
+    hitm = eng.hit_counts() > 0
+    med = float(np.median(rel[hitm])) if hitm.any() else None
+    flux_err = {"median_relative_error": med,
+                "p90_relative_error": float(np.quantile(rel[hitm], 0.9)) if hitm.any() else None,
+                "primitives_hit": int(hitm.sum()), "primitives": int(len(rel)),
+                "rays_for_1pct_median": int(R * (med / 0.01) ** 2) if med else None,
+                "gpu_vs_cpu": "bit-identical hit counts and tallies (tests/test_gpu_parity.py)"}
+
     # the plain GPU baseline: the same trace as a non-persistent launch
     plain = None
     if not args.no_plain:
@@ -505,7 +517,7 @@ def run_ours(args):
                 "data": "synthetic", "config": config_dict(h, R), "clocks": clocks, "roofline": roof,
                 "roofline_l2": roof_l2,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps, "adjoint": adj,
-                "plain_gpu": plain, "batch": batch, "rough_field": rough,
+                "plain_gpu": plain, "batch": batch, "rough_field": rough, "flux_error": flux_err,
                 "wall_s_timed_region": wall,
                 "tally_per_step": {"segments": seg, "hitc": statistics.mean(t.hitc for t in tallies),
                                    "truncated": max(t.truncated for t in tallies),
