@@ -121,7 +121,13 @@ typedef struct rtg_launch_config {
   int32_t stack_depth;       /* traversal stack entries, 32, 64 or 256; 0 = the smallest that holds the
                                 tree (a smaller request than the tree needs is raised to that) */
   int32_t scheduling;        /* RTG_SCHED_* */
+  int32_t leaf_tests;        /* RTG_LEAF_*: when the primitives of a leaf the ray reaches are tested */
 } rtg_launch_config;
+/* leaf_tests: on the spot, or postponed until every lane of the warp holds a
+ * leaf (Aila and Laine's while-while traversal; megakernel and plain
+ * schedules, forward traces) */
+#define RTG_LEAF_IMMEDIATE 0
+#define RTG_LEAF_POSTPONED 1
 
 /* Fills *cfg with rti's defaults. */
 RTG_API void rtg_config_default(rtg_config* cfg);

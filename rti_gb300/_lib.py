@@ -52,6 +52,8 @@ RTG_SCHED_MEGAKERNEL = 0
 RTG_SCHED_WAVEFRONT = 1
 RTG_SCHED_PLAIN = 2
 RTG_TREE_KARRAS = 0
+RTG_LEAF_IMMEDIATE = 0
+RTG_LEAF_POSTPONED = 1
 RTG_TREE_PLOC = 1
 
 
@@ -87,7 +89,7 @@ class RtgDeviceView(C.Structure):
 
 class RtgLaunchConfig(C.Structure):
     _fields_ = [("threads_per_block", C.c_int32), ("packet", C.c_int32), ("stack_depth", C.c_int32),
-                ("scheduling", C.c_int32)]
+                ("scheduling", C.c_int32), ("leaf_tests", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -168,7 +168,7 @@ struct rtg_context {
   bool traced = false;
   bool finalized = false;
   float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
-  rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL};
+  rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL, RTG_LEAF_IMMEDIATE};
   rtg::Wavefront wf;
   std::string err;
 };

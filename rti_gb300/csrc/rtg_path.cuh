@@ -76,7 +76,13 @@ __device__ __forceinline__ void test_leaf(const SceneView& s, uint32_t ref, cons
 
 // Closest primitive hit; returns false when nothing is hit.  errs counts
 // stack overflows and iteration-limit trips (both end the query).
-template <int STACK>
+// POSTPONE = false: a leaf child whose box the ray enters is tested on the
+// spot.  POSTPONE = true (Aila and Laine, HPG 2009, "while-while"): a lane
+// keeps one such leaf pending and walks on through inner nodes until every
+// lane of the warp holds a pending leaf (or has no inner node left), then the
+// warp tests the pending leaves together; the closest hit is the same, only
+// the lanes that run the primitive tests together change.
+template <int STACK, bool POSTPONE>
 __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& bt, int& bid, uint32_t& bref,
                             unsigned long long& errs) {
   Ray r;
@@ -90,43 +96,100 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   int sp = 0;
   uint32_t cur = s.root;
   const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
-  for (int64_t it = 0;; ++it) {
-    if (it > max_iter) {
-      errs += 1;
-      break;
-    }
-    const Node* nd = s.nodes + cur;
-    const float4 a = __ldg(&nd->a);
-    const float4 b = __ldg(&nd->b);
-    const float4 c = __ldg(&nd->c);
-    const uint4 ch = __ldg(&nd->d);
-    float tn0, tn1;
-    bool h0 = slab(a.x, a.y, b.x, b.y, c.x, c.y, r, bt, tn0);
-    bool h1 = slab(a.z, a.w, b.z, b.w, c.z, c.w, r, bt, tn1);
-    if (h0 && (ch.x & kLeafBit)) {
-      test_leaf(s, ch.x, r, tnear, bt, bid, bref);
-      h0 = false;
-    }
-    if (h1 && (ch.y & kLeafBit)) {
-      test_leaf(s, ch.y, r, tnear, bt, bid, bref);
-      h1 = false;
-    }
-    if (h0 && h1) {
-      uint32_t nearc = tn0 <= tn1 ? ch.x : ch.y;
-      uint32_t farc = tn0 <= tn1 ? ch.y : ch.x;
-      if (sp < STACK) {
-        stack[sp++] = farc;
-      } else {
+  if (!POSTPONE) {
+    for (int64_t it = 0;; ++it) {
+      if (it > max_iter) {
         errs += 1;
+        break;
       }
-      cur = nearc;
-    } else if (h0) {
-      cur = ch.x;
-    } else if (h1) {
-      cur = ch.y;
-    } else {
-      if (sp == 0) break;
-      cur = stack[--sp];
+      const Node* nd = s.nodes + cur;
+      const float4 a = __ldg(&nd->a);
+      const float4 b = __ldg(&nd->b);
+      const float4 c = __ldg(&nd->c);
+      const uint4 ch = __ldg(&nd->d);
+      float tn0, tn1;
+      bool h0 = slab(a.x, a.y, b.x, b.y, c.x, c.y, r, bt, tn0);
+      bool h1 = slab(a.z, a.w, b.z, b.w, c.z, c.w, r, bt, tn1);
+      if (h0 && (ch.x & kLeafBit)) {
+        test_leaf(s, ch.x, r, tnear, bt, bid, bref);
+        h0 = false;
+      }
+      if (h1 && (ch.y & kLeafBit)) {
+        test_leaf(s, ch.y, r, tnear, bt, bid, bref);
+        h1 = false;
+      }
+      if (h0 && h1) {
+        uint32_t nearc = tn0 <= tn1 ? ch.x : ch.y;
+        uint32_t farc = tn0 <= tn1 ? ch.y : ch.x;
+        if (sp < STACK) {
+          stack[sp++] = farc;
+        } else {
+          errs += 1;
+        }
+        cur = nearc;
+      } else if (h0) {
+        cur = ch.x;
+      } else if (h1) {
+        cur = ch.y;
+      } else {
+        if (sp == 0) break;
+        cur = stack[--sp];
+      }
+    }
+    return bid != INT_MAX;
+  }
+  // while-while: leaves travel through `cur` and the stack like inner nodes
+  constexpr uint32_t kNone = 0xFFFFFFFFu;
+  uint32_t leaf = kNone;
+  int64_t it = 0;
+  auto pop = [&]() -> uint32_t { return sp > 0 ? stack[--sp] : kNone; };
+  while (cur != kNone) {
+    // inner nodes until every lane of the warp holds a pending leaf
+    while (cur != kNone && !(cur & kLeafBit)) {
+      if (++it > max_iter) {
+        errs += 1;
+        cur = kNone;
+        break;
+      }
+      const Node* nd = s.nodes + cur;
+      const float4 a = __ldg(&nd->a);
+      const float4 b = __ldg(&nd->b);
+      const float4 c = __ldg(&nd->c);
+      const uint4 ch = __ldg(&nd->d);
+      float tn0, tn1;
+      const bool h0 = slab(a.x, a.y, b.x, b.y, c.x, c.y, r, bt, tn0);
+      const bool h1 = slab(a.z, a.w, b.z, b.w, c.z, c.w, r, bt, tn1);
+      if (h0 && h1) {
+        const bool first = tn0 <= tn1;
+        if (sp < STACK) stack[sp++] = first ? ch.y : ch.x;
+        else errs += 1;
+        cur = first ? ch.x : ch.y;
+      } else if (h0) {
+        cur = ch.x;
+      } else if (h1) {
+        cur = ch.y;
+      } else {
+        cur = pop();
+      }
+      if (cur != kNone && (cur & kLeafBit) && leaf == kNone) {
+        leaf = cur;
+        cur = pop();
+      }
+      if (!__any_sync(__activemask(), leaf == kNone)) break;
+    }
+    // the pending leaf, and any leaf reached right after it
+    while (leaf != kNone) {
+      if (++it > max_iter) {
+        errs += 1;
+        cur = kNone;
+        break;
+      }
+      test_leaf(s, leaf, r, tnear, bt, bid, bref);
+      leaf = kNone;
+      if (cur != kNone && (cur & kLeafBit)) {
+        leaf = cur;
+        cur = pop();
+      }
     }
   }
   return bid != INT_MAX;
@@ -196,7 +259,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // its job's parameters (scene, configuration, accumulators); the counters and
 // the abort flag are the batch's (p0).  TPB threads per block and 1024 / TPB
 // resident blocks per SM as the register target (64 registers per thread).
-template <int M, bool Batched, int TPB, int STACK>
+template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false>
 __global__ void __launch_bounds__(TPB, 1024 / TPB)
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
@@ -311,7 +374,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
     float th, tb = 0.0f;
     int hid;
     uint32_t href;
-    const bool hit = closest_hit<STACK>(pp->s, o, d, pp->tnear, th, hid, href, c_err);
+    const bool hit = closest_hit<STACK, POSTPONE>(pp->s, o, d, pp->tnear, th, hid, href, c_err);
     const int axis = boundary_exit(*pp, o, d, tb);
     if (hit && (axis < 0 || th <= tb)) {
       float4 nn;

@@ -16,7 +16,7 @@ __global__ void closest_hit_kernel(const SceneView s, const float* __restrict__ 
   int id;
   uint32_t ref;
   unsigned long long e = 0;
-  if (closest_hit<256>(s, mk3(r[0], r[1], r[2]), mk3(r[3], r[4], r[5]), tnear, t, id, ref, e)) {
+  if (closest_hit<256, false>(s, mk3(r[0], r[1], r[2]), mk3(r[3], r[4], r[5]), tnear, t, id, ref, e)) {
     prim[i] = id;
     tout[i] = t;
   } else {
@@ -28,15 +28,20 @@ __global__ void closest_hit_kernel(const SceneView s, const float* __restrict__ 
 
 using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_t*, int);
 
-template <int TPB>
+template <int TPB, bool POSTPONE>
 PathKernel forward_kernel(int stack) {
-  if (stack <= 32) return trace_paths_kernel<kModeForward, false, TPB, 32>;
-  if (stack <= 64) return trace_paths_kernel<kModeForward, false, TPB, 64>;
-  return trace_paths_kernel<kModeForward, false, TPB, 256>;
+  if (stack <= 32) return trace_paths_kernel<kModeForward, false, TPB, 32, POSTPONE>;
+  if (stack <= 64) return trace_paths_kernel<kModeForward, false, TPB, 64, POSTPONE>;
+  return trace_paths_kernel<kModeForward, false, TPB, 256, POSTPONE>;
+}
+
+template <int TPB>
+PathKernel forward_kernel(int stack, bool postpone) {
+  return postpone ? forward_kernel<TPB, true>(stack) : forward_kernel<TPB, false>(stack);
 }
 
 // The adjoint replays run with 128 threads and a 64- or 256-entry stack.
-PathKernel pick_kernel(int mode, int tpb, int stack, int& tpb_out) {
+PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, int& tpb_out) {
   if (mode == kModeAdjGlobal) {
     tpb_out = 128;
     return stack <= 64 ? trace_paths_kernel<kModeAdjGlobal, false, 128, 64>
@@ -48,10 +53,10 @@ PathKernel pick_kernel(int mode, int tpb, int stack, int& tpb_out) {
                        : trace_paths_kernel<kModeAdjField, false, 128, 256>;
   }
   tpb_out = tpb;
-  if (tpb == 64) return forward_kernel<64>(stack);
-  if (tpb == 256) return forward_kernel<256>(stack);
+  if (tpb == 64) return forward_kernel<64>(stack, postpone);
+  if (tpb == 256) return forward_kernel<256>(stack, postpone);
   tpb_out = 128;
-  return forward_kernel<128>(stack);
+  return forward_kernel<128>(stack, postpone);
 }
 
 }  // namespace
@@ -73,6 +78,8 @@ int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc) {
   if (lc.scheduling != RTG_SCHED_MEGAKERNEL && lc.scheduling != RTG_SCHED_WAVEFRONT &&
       lc.scheduling != RTG_SCHED_PLAIN)
     return bad("scheduling must be RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT or RTG_SCHED_PLAIN");
+  if (lc.leaf_tests != RTG_LEAF_IMMEDIATE && lc.leaf_tests != RTG_LEAF_POSTPONED)
+    return bad("leaf_tests must be RTG_LEAF_IMMEDIATE or RTG_LEAF_POSTPONED");
   return RTG_OK;
 }
 
@@ -113,7 +120,7 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
     return launch_wavefront(ctx, p, wf.one_job.p, wf.one_prefix.p, 1, nrays, st, lc, ctx->g.depth);
   }
   int tpb = 128, sms = 0, per_sm = 0;
-  PathKernel kern = pick_kernel(mode, lc.threads_per_block, stack, tpb);
+  PathKernel kern = pick_kernel(mode, lc.threads_per_block, stack, lc.leaf_tests == RTG_LEAF_POSTPONED, tpb);
   p.plain = mode == kModeForward && lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));

@@ -8,11 +8,16 @@ namespace {
 
 using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_t*, int);
 
-template <int TPB>
+template <int TPB, bool POSTPONE>
 PathKernel batched_kernel(int stack) {
-  if (stack <= 32) return trace_paths_kernel<kModeForward, true, TPB, 32>;
-  if (stack <= 64) return trace_paths_kernel<kModeForward, true, TPB, 64>;
-  return trace_paths_kernel<kModeForward, true, TPB, 256>;
+  if (stack <= 32) return trace_paths_kernel<kModeForward, true, TPB, 32, POSTPONE>;
+  if (stack <= 64) return trace_paths_kernel<kModeForward, true, TPB, 64, POSTPONE>;
+  return trace_paths_kernel<kModeForward, true, TPB, 256, POSTPONE>;
+}
+
+template <int TPB>
+PathKernel batched_kernel(int stack, bool postpone) {
+  return postpone ? batched_kernel<TPB, true>(stack) : batched_kernel<TPB, false>(stack);
 }
 
 }  // namespace
@@ -27,8 +32,9 @@ int launch_trace_batched(rtg_context* ctx, const TraceParams& p0_in, const Trace
   p0.packet = lc.packet;
   p0.plain = lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
   int tpb = lc.threads_per_block, sms = 0, per_sm = 0;
-  PathKernel kern = tpb == 64 ? batched_kernel<64>(stack) : tpb == 256 ? batched_kernel<256>(stack)
-                                                                       : batched_kernel<128>(stack);
+  const bool pp = lc.leaf_tests == RTG_LEAF_POSTPONED;
+  PathKernel kern = tpb == 64 ? batched_kernel<64>(stack, pp) : tpb == 256 ? batched_kernel<256>(stack, pp)
+                                                                           : batched_kernel<128>(stack, pp);
   if (tpb != 64 && tpb != 256) tpb = 128;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));

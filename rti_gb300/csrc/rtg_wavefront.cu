@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(TPB) wf_extend_kernel(const TraceParams* __res
     float th;
     int hid;
     uint32_t href;
-    const bool hit = closest_hit<STACK>(pp->s, o, d, pp->tnear, th, hid, href, c_err);
+    const bool hit = closest_hit<STACK, false>(pp->s, o, d, pp->tnear, th, hid, href, c_err);
     b.ht[i] = th;
     b.hid[i] = hit ? hid : -1;
     b.href[i] = href;

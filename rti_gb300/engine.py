@@ -164,8 +164,8 @@ class Engine:
         return lc
 
     def set_launch_config(self, threads_per_block: int = 128, packet: int = 1, stack_depth: int = 0,
-                          scheduling: int = L.RTG_SCHED_MEGAKERNEL):
-        lc = L.RtgLaunchConfig(threads_per_block, packet, stack_depth, scheduling)
+                          scheduling: int = L.RTG_SCHED_MEGAKERNEL, leaf_tests: int = L.RTG_LEAF_IMMEDIATE):
+        lc = L.RtgLaunchConfig(threads_per_block, packet, stack_depth, scheduling, leaf_tests)
         self._check(self._L.rtg_set_launch_config(self._h, C.byref(lc)))
 
     @property

@@ -14,7 +14,8 @@ pytestmark = pytest.mark.gpu
 S1_RTOL = 1e-9
 MK, WF, PL = 0, 1, 2
 CONFIGS = [(64, 1, 0, MK), (256, 8, 0, MK), (128, 32, 256, MK), (128, 1, 32, MK), (128, 1, 0, WF),
-           (256, 1, 256, WF), (64, 1, 64, WF), (128, 1, 0, PL), (256, 1, 64, PL)]
+           (256, 1, 256, WF), (64, 1, 64, WF), (128, 1, 0, PL), (256, 1, 64, PL),
+           (128, 1, 0, MK, 1), (256, 8, 256, MK, 1), (128, 1, 0, PL, 1)]
 
 
 @pytest.fixture(scope="module")
@@ -81,7 +82,7 @@ def test_wavefront_truncation_field_and_reflective_box(eng):
     eng.set_launch_config()
     ref = _run(eng, 40000, 8)
     assert ref[2].truncated > 0
-    for cfg in ((128, 1, 0, WF), (128, 1, 0, PL)):
+    for cfg in ((128, 1, 0, WF), (128, 1, 0, PL), (128, 1, 0, MK, 1)):
         eng.set_launch_config(*cfg)
         _same(ref, _run(eng, 40000, 8))
     # a sample larger than the queue capacity is generated over several waves
@@ -126,7 +127,7 @@ def test_batch_wavefront_and_autotune(rtg_lib):
         b.synchronize()
         ref = [b.results(j) for j in range(len(b))]
         t_ref = b.tally()
-        for cfg in [(128, 1, 0, WF), (64, 8, 256, MK), (256, 32, 0, MK), (128, 1, 0, PL)]:
+        for cfg in [(128, 1, 0, WF), (64, 8, 256, MK), (256, 32, 0, MK), (128, 1, 0, PL), (128, 8, 0, MK, 1)]:
             b.set_launch_config(*cfg)
             b.run(use_graph=True)
             b.synchronize()
