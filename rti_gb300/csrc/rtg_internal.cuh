@@ -239,6 +239,29 @@ void dfree(DBuf<T>& b) {
   b.p = nullptr;
   b.n = 0;
 }
+// Temporaries of a build step: stream-ordered allocations from the device's
+// memory pool, released on the same stream without the device-wide
+// synchronisation of cudaFree.
+template <typename T>
+int talloc(rtg_context* ctx, DBuf<T>& b, size_t n, cudaStream_t st, const char* what) {
+  b.p = nullptr;
+  b.n = 0;
+  if (n == 0) return RTG_OK;
+  cudaError_t e = cudaMallocAsync((void**)&b.p, n * sizeof(T), st);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    cudaGetLastError();
+    return set_error(ctx, RTG_ERR_OUT_OF_MEMORY, std::string("cudaMallocAsync failed for ") + what);
+  }
+  b.n = n;
+  return RTG_OK;
+}
+template <typename T>
+void tfree(DBuf<T>& b, cudaStream_t st) {
+  if (b.p) cudaFreeAsync(b.p, st);
+  b.p = nullptr;
+  b.n = 0;
+}
 
 // device helpers shared by the kernels
 __host__ __device__ inline int num_sms_hint() { return 152; }

@@ -469,14 +469,14 @@ int tree_depth(rtg_context* ctx, cudaStream_t st) {
     return RTG_OK;
   }
   DBuf<unsigned int> dd;
-  RTG_TRY(dalloc(ctx, dd, 1, "tree depth"));
+  RTG_TRY(talloc(ctx, dd, 1, st, "tree depth"));
   unsigned int h = 0;
   cudaMemsetAsync(dd.p, 0, sizeof(unsigned int), st);
   depth_kernel<<<blocks_for(np, 256), 256, 0, st>>>(np, g.parent.p, dd.p);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dd.p, sizeof h, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  dfree(dd);
+  tfree(dd, st);
   if (e != cudaSuccess) return check_cuda(ctx, e, "tree depth");
   if (h > 256) return set_error(ctx, RTG_ERR_INTERNAL, "LBVH deeper than 256 levels");
   g.depth = (int32_t)h;
@@ -490,11 +490,11 @@ int validate_tree(rtg_context* ctx, cudaStream_t st) {
   const int64_t ni = np - 1;
   DBuf<unsigned int> pi, pd, pt;
   DBuf<unsigned long long> err;
-  auto cleanup = [&]() { dfree(pi); dfree(pd); dfree(pt); dfree(err); };
-  int rc = dalloc(ctx, pi, (size_t)ni, "tree check");
-  if (rc == RTG_OK) rc = dalloc(ctx, pd, (size_t)(g.nd ? g.nd : 1), "tree check");
-  if (rc == RTG_OK) rc = dalloc(ctx, pt, (size_t)(g.nt ? g.nt : 1), "tree check");
-  if (rc == RTG_OK) rc = dalloc(ctx, err, 1, "tree check");
+  auto cleanup = [&]() { tfree(pi, st); tfree(pd, st); tfree(pt, st); tfree(err, st); };
+  int rc = talloc(ctx, pi, (size_t)ni, st, "tree check");
+  if (rc == RTG_OK) rc = talloc(ctx, pd, (size_t)(g.nd ? g.nd : 1), st, "tree check");
+  if (rc == RTG_OK) rc = talloc(ctx, pt, (size_t)(g.nt ? g.nt : 1), st, "tree check");
+  if (rc == RTG_OK) rc = talloc(ctx, err, 1, st, "tree check");
   if (rc != RTG_OK) { cleanup(); return rc; }
   cudaMemsetAsync(pi.p, 0, ni * sizeof(unsigned int), st);
   cudaMemsetAsync(pd.p, 0, pd.n * sizeof(unsigned int), st);
@@ -527,25 +527,25 @@ int build_ploc(rtg_context* ctx, const uint32_t* d_sorted_prim, cudaStream_t st)
   DBuf<uint64_t> state;  // [0] clusters, [1] nodes allocated, [2] stall flag
   auto cleanup = [&]() {
     for (int q = 0; q < 2; ++q) {
-      dfree(cid[q]);
-      dfree(blo[q]);
-      dfree(bhi[q]);
+      tfree(cid[q], st);
+      tfree(blo[q], st);
+      tfree(bhi[q], st);
     }
-    dfree(nn);
-    dfree(packed);
-    dfree(total);
-    dfree(state);
+    tfree(nn, st);
+    tfree(packed, st);
+    tfree(total, st);
+    tfree(state, st);
   };
   int rc = RTG_OK;
   for (int q = 0; q < 2 && rc == RTG_OK; ++q) {
-    rc = dalloc(ctx, cid[q], (size_t)n, "PLOC clusters");
-    if (rc == RTG_OK) rc = dalloc(ctx, blo[q], (size_t)n, "PLOC boxes");
-    if (rc == RTG_OK) rc = dalloc(ctx, bhi[q], (size_t)n, "PLOC boxes");
+    rc = talloc(ctx, cid[q], (size_t)n, st, "PLOC clusters");
+    if (rc == RTG_OK) rc = talloc(ctx, blo[q], (size_t)n, st, "PLOC boxes");
+    if (rc == RTG_OK) rc = talloc(ctx, bhi[q], (size_t)n, st, "PLOC boxes");
   }
-  if (rc == RTG_OK) rc = dalloc(ctx, nn, (size_t)n, "PLOC neighbours");
-  if (rc == RTG_OK) rc = dalloc(ctx, packed, (size_t)n, "PLOC scan");
-  if (rc == RTG_OK) rc = dalloc(ctx, total, 1, "PLOC totals");
-  if (rc == RTG_OK) rc = dalloc(ctx, state, 3, "PLOC state");
+  if (rc == RTG_OK) rc = talloc(ctx, nn, (size_t)n, st, "PLOC neighbours");
+  if (rc == RTG_OK) rc = talloc(ctx, packed, (size_t)n, st, "PLOC scan");
+  if (rc == RTG_OK) rc = talloc(ctx, total, 1, st, "PLOC totals");
+  if (rc == RTG_OK) rc = talloc(ctx, state, 3, st, "PLOC state");
   if (rc != RTG_OK) {
     cleanup();
     return rc;
@@ -624,10 +624,10 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
     return RTG_OK;
   }
   DBuf<float> node_box;
-  RTG_TRY(dalloc(ctx, node_box, (size_t)(6 * (np - 1)), "node boxes"));
+  RTG_TRY(talloc(ctx, node_box, (size_t)(6 * (np - 1)), st, "node boxes"));
   DBuf<unsigned long long> err;
-  int rc = dalloc(ctx, err, 1, "refit status");
-  if (rc != RTG_OK) { dfree(node_box); return rc; }
+  int rc = talloc(ctx, err, 1, st, "refit status");
+  if (rc != RTG_OK) { tfree(node_box, st); return rc; }
   RTG_TRY(dalloc(ctx, g.refit_flags, (size_t)(np - 1), "refit flags"));
   cudaMemsetAsync(g.refit_flags.p, 0, sizeof(unsigned int) * (np - 1), st);
   cudaMemsetAsync(err.p, 0, sizeof(unsigned long long), st);
@@ -638,8 +638,8 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
   unsigned long long herr = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err.p, sizeof herr, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  dfree(node_box);
-  dfree(err);
+  tfree(node_box, st);
+  tfree(err, st);
   if (e != cudaSuccess) return check_cuda(ctx, e, "LBVH refit");
   if (herr) return set_error(ctx, RTG_ERR_INTERNAL, "LBVH refit exceeded its depth limit");
   return RTG_OK;
@@ -654,25 +654,25 @@ int build_lbvh(rtg_context* ctx) {
   if (np <= 0) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no primitives");
   if (np > (int64_t)kSlotMask) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "too many primitives");
   DBuf<uint32_t> cb, keys, vals, tk, tv, rank;
-  auto cleanup = [&]() { dfree(cb); dfree(keys); dfree(vals); dfree(tk); dfree(tv); dfree(rank); };
+  auto cleanup = [&]() { tfree(cb, st); tfree(keys, st); tfree(vals, st); tfree(tk, st); tfree(tv, st); tfree(rank, st); };
   int rc = RTG_OK;
   do {
-    if ((rc = dalloc(ctx, cb, 6, "centroid bounds")) != RTG_OK) break;
+    if ((rc = talloc(ctx, cb, 6, st, "centroid bounds")) != RTG_OK) break;
     const uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
     if (cudaMemcpyAsync(cb.p, init, sizeof init, cudaMemcpyHostToDevice, st) != cudaSuccess) {
       rc = check_cuda(ctx, cudaGetLastError(), "centroid bounds init");
       break;
     }
     if ((rc = run_bounds(ctx, cb.p, st)) != RTG_OK) break;
-    if ((rc = dalloc(ctx, keys, (size_t)np, "morton keys")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, vals, (size_t)np, "morton values")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, tk, (size_t)np, "sort scratch")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, tv, (size_t)np, "sort scratch")) != RTG_OK) break;
+    if ((rc = talloc(ctx, keys, (size_t)np, st, "morton keys")) != RTG_OK) break;
+    if ((rc = talloc(ctx, vals, (size_t)np, st, "morton values")) != RTG_OK) break;
+    if ((rc = talloc(ctx, tk, (size_t)np, st, "sort scratch")) != RTG_OK) break;
+    if ((rc = talloc(ctx, tv, (size_t)np, st, "sort scratch")) != RTG_OK) break;
     morton_kernel<<<blocks_for(np, 256), 256, 0, st>>>(g.prim_lo.p, g.prim_hi.p, np, cb.p, keys.p, vals.p);
     if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "morton"); break; }
     if ((rc = radix_sort_pairs(ctx, keys.p, vals.p, tk.p, tv.p, np, 30, st)) != RTG_OK) break;
     // disc slot = number of discs before this sorted position
-    if ((rc = dalloc(ctx, rank, (size_t)np, "disc ranks")) != RTG_OK) break;
+    if ((rc = talloc(ctx, rank, (size_t)np, st, "disc ranks")) != RTG_OK) break;
     disc_flag_kernel<<<blocks_for(np, 256), 256, 0, st>>>(vals.p, np, g.nd, rank.p);
     if ((rc = exclusive_scan_u32(ctx, rank.p, np, nullptr, st)) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.disc_cr, (size_t)(g.nd ? g.nd : 1), "disc slots")) != RTG_OK) break;
@@ -724,8 +724,8 @@ int refit_lbvh(rtg_context* ctx) {
   // keep the leaf order: recompute slot data from the sorted primitive order
   const int64_t np = g.nd + g.nt;
   DBuf<uint32_t> rank, order;
-  int rc = dalloc(ctx, rank, (size_t)np, "disc ranks");
-  if (rc == RTG_OK) rc = dalloc(ctx, order, (size_t)np, "leaf order");
+  int rc = talloc(ctx, rank, (size_t)np, st, "disc ranks");
+  if (rc == RTG_OK) rc = talloc(ctx, order, (size_t)np, st, "leaf order");
   if (rc == RTG_OK) {
     cudaMemcpyAsync(order.p, g.leaf_prim.p, np * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
     disc_flag_kernel<<<blocks_for(np, 256), 256, 0, st>>>(order.p, np, g.nd, rank.p);
@@ -733,8 +733,8 @@ int refit_lbvh(rtg_context* ctx) {
   }
   if (rc == RTG_OK) rc = run_slots_and_refit(ctx, order.p, rank.p, st);
   cudaStreamSynchronize(st);
-  dfree(rank);
-  dfree(order);
+  tfree(rank, st);
+  tfree(order, st);
   return rc;
 }
 

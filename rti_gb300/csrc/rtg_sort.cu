@@ -149,7 +149,7 @@ int radix_sort_pairs(rtg_context* ctx, uint32_t* d_keys, uint32_t* d_vals, uint3
   if (n <= 1) return RTG_OK;
   const int64_t tiles = (n + kRsTile - 1) / kRsTile;
   DBuf<uint32_t> hist;
-  RTG_TRY(dalloc(ctx, hist, (size_t)(256 * tiles), "radix histogram"));
+  RTG_TRY(talloc(ctx, hist, (size_t)(256 * tiles), st, "radix histogram"));
   uint32_t *kin = d_keys, *vin = d_vals, *kout = d_tmp_keys, *vout = d_tmp_vals;
   int passes = (bits + 7) / 8;
   int rc = RTG_OK;
@@ -171,7 +171,7 @@ int radix_sort_pairs(rtg_context* ctx, uint32_t* d_keys, uint32_t* d_vals, uint3
     else if (e2 != cudaSuccess) rc = check_cuda(ctx, e2, "radix copy values");
   }
   cudaError_t es = cudaStreamSynchronize(st);
-  dfree(hist);
+  tfree(hist, st);
   if (rc == RTG_OK && es != cudaSuccess) rc = check_cuda(ctx, es, "radix sort");
   return rc;
 }

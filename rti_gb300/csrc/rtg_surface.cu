@@ -376,16 +376,16 @@ int build_neighbors(rtg_context* ctx) {
   const int64_t ncells = (int64_t)grid.dim[0] * grid.dim[1] * grid.dim[2];
   DBuf<uint32_t> keys, vals, tk, tv, cs, ce;
   DBuf<int64_t> counts;
-  auto cleanup = [&]() { dfree(keys); dfree(vals); dfree(tk); dfree(tv); dfree(cs); dfree(ce); dfree(counts); };
+  auto cleanup = [&]() { tfree(keys, st); tfree(vals, st); tfree(tk, st); tfree(tv, st); tfree(cs, st); tfree(ce, st); tfree(counts, st); };
   int rc = RTG_OK;
   do {
-    if ((rc = dalloc(ctx, keys, (size_t)nd, "grid keys")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, vals, (size_t)nd, "grid ids")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, tk, (size_t)nd, "sort scratch")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, tv, (size_t)nd, "sort scratch")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, cs, (size_t)ncells, "cell starts")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, ce, (size_t)ncells, "cell ends")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, counts, (size_t)(nd + 1), "neighbour counts")) != RTG_OK) break;
+    if ((rc = talloc(ctx, keys, (size_t)nd, st, "grid keys")) != RTG_OK) break;
+    if ((rc = talloc(ctx, vals, (size_t)nd, st, "grid ids")) != RTG_OK) break;
+    if ((rc = talloc(ctx, tk, (size_t)nd, st, "sort scratch")) != RTG_OK) break;
+    if ((rc = talloc(ctx, tv, (size_t)nd, st, "sort scratch")) != RTG_OK) break;
+    if ((rc = talloc(ctx, cs, (size_t)ncells, st, "cell starts")) != RTG_OK) break;
+    if ((rc = talloc(ctx, ce, (size_t)ncells, st, "cell ends")) != RTG_OK) break;
+    if ((rc = talloc(ctx, counts, (size_t)(nd + 1), st, "neighbour counts")) != RTG_OK) break;
     cell_key_kernel<<<blocks_for(nd, 256), 256, 0, st>>>(g.disc_cr_by_id.p, nd, grid, keys.p, vals.p);
     int bits = 1;
     while (bits < 32 && ((int64_t)1 << bits) < ncells) ++bits;
