@@ -39,9 +39,8 @@ struct DevTally {
 
 // Read-only view of a scene for the kernels.
 struct SceneView {
-  // discs in LBVH (slot) order: centre + radius, normal + original id bits
-  const float4* disc_cr;
-  const float4* disc_n;
+  // discs in LBVH (slot) order, 32 B each: (centre, radius), (normal, original id bits)
+  const float4* disc;
   int32_t nd;
   // triangles in slot order: v0 + original id bits, e1, e2 (3 float4 per slot)
   const float4* tri;
@@ -110,7 +109,8 @@ struct Geometry {
   DBuf<float4> tri_v;      // nv vertices (xyz, 0)
   DBuf<uint32_t> tri_idx;  // nt*3
   // slot-ordered copies
-  DBuf<float4> disc_cr, disc_n, tri, tri_n;
+  DBuf<float4> disc;       // 2 per slot: (centre, radius), (normal, id bits)
+  DBuf<float4> tri, tri_n;
   DBuf<Node> nodes;
   DBuf<uint32_t> leaf_ref;    // per sorted leaf i: child reference
   DBuf<int32_t> leaf_prim;    // per sorted leaf i: original primitive id

@@ -116,8 +116,8 @@ __global__ void disc_flag_kernel(const uint32_t* __restrict__ sorted_prim, int64
 __global__ void slots_kernel(const uint32_t* __restrict__ sorted_prim, const uint32_t* __restrict__ disc_rank,
                              int64_t np, int64_t nd, const float4* __restrict__ dcr_id,
                              const float4* __restrict__ dn_id, const float4* __restrict__ tv,
-                             const uint32_t* __restrict__ tidx, float4* __restrict__ dcr,
-                             float4* __restrict__ dn, float4* __restrict__ tri, float4* __restrict__ tri_n,
+                             const uint32_t* __restrict__ tidx, float4* __restrict__ disc,
+                             float4* __restrict__ tri, float4* __restrict__ tri_n,
                              uint32_t* __restrict__ leaf_ref, int32_t* __restrict__ leaf_prim) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= np) return;
@@ -126,8 +126,8 @@ __global__ void slots_kernel(const uint32_t* __restrict__ sorted_prim, const uin
   leaf_prim[i] = (int32_t)p;
   if (p < (uint32_t)nd) {
     float4 n = dn_id[p];
-    dcr[ds] = dcr_id[p];
-    dn[ds] = make_float4(n.x, n.y, n.z, __int_as_float((int)p));
+    disc[2 * (int64_t)ds] = dcr_id[p];
+    disc[2 * (int64_t)ds + 1] = make_float4(n.x, n.y, n.z, __int_as_float((int)p));
     leaf_ref[i] = kLeafBit | ds;
   } else {
     uint32_t ts = (uint32_t)i - ds;
@@ -342,7 +342,7 @@ __device__ __forceinline__ void child_box(uint32_t ref, const float4* __restrict
                                           float* hi) {
   if (ref & kLeafBit) {
     uint32_t slot = ref & kSlotMask;
-    int p = (ref & kTriBit) ? __float_as_int(tri[3 * slot].w) : __float_as_int(dn[slot].w);
+    int p = (ref & kTriBit) ? __float_as_int(tri[3 * slot].w) : __float_as_int(dn[2 * (int64_t)slot + 1].w);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       lo[a] = plo[3 * (int64_t)p + a];
@@ -613,13 +613,13 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
   const int64_t np = g.nd + g.nt;
   if (d_sorted_prim) {
     slots_kernel<<<blocks_for(np, 256), 256, 0, st>>>(d_sorted_prim, d_disc_rank, np, g.nd, g.disc_cr_by_id.p,
-                                                      g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc_cr.p,
-                                                      g.disc_n.p, g.tri.p, g.tri_n.p, g.leaf_ref.p,
+                                                      g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc.p,
+                                                      g.tri.p, g.tri_n.p, g.leaf_ref.p,
                                                       g.leaf_prim.p);
     RTG_CUDA(ctx, cudaGetLastError());
   }
   if (np == 1) {
-    single_leaf_kernel<<<1, 1, 0, st>>>(g.leaf_ref.p, g.disc_n.p, g.tri.p, g.prim_lo.p, g.prim_hi.p, g.nodes.p);
+    single_leaf_kernel<<<1, 1, 0, st>>>(g.leaf_ref.p, g.disc.p, g.tri.p, g.prim_lo.p, g.prim_hi.p, g.nodes.p);
     RTG_CUDA(ctx, cudaGetLastError());
     return RTG_OK;
   }
@@ -631,7 +631,7 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
   RTG_TRY(dalloc(ctx, g.refit_flags, (size_t)(np - 1), "refit flags"));
   cudaMemsetAsync(g.refit_flags.p, 0, sizeof(unsigned int) * (np - 1), st);
   cudaMemsetAsync(err.p, 0, sizeof(unsigned long long), st);
-  refit_kernel<<<blocks_for(np, 256), 256, 0, st>>>(np, g.leaf_ref.p, g.parent.p, g.disc_n.p, g.tri.p,
+  refit_kernel<<<blocks_for(np, 256), 256, 0, st>>>(np, g.leaf_ref.p, g.parent.p, g.disc.p, g.tri.p,
                                                     g.prim_lo.p, g.prim_hi.p, g.nodes.p, node_box.p,
                                                     g.refit_flags.p, err.p);
   cudaError_t e = cudaGetLastError();
@@ -675,8 +675,7 @@ int build_lbvh(rtg_context* ctx) {
     if ((rc = talloc(ctx, rank, (size_t)np, st, "disc ranks")) != RTG_OK) break;
     disc_flag_kernel<<<blocks_for(np, 256), 256, 0, st>>>(vals.p, np, g.nd, rank.p);
     if ((rc = exclusive_scan_u32(ctx, rank.p, np, nullptr, st)) != RTG_OK) break;
-    if ((rc = dalloc(ctx, g.disc_cr, (size_t)(g.nd ? g.nd : 1), "disc slots")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, g.disc_n, (size_t)(g.nd ? g.nd : 1), "disc slots")) != RTG_OK) break;
+    if ((rc = dalloc(ctx, g.disc, (size_t)(2 * (g.nd ? g.nd : 1)), "disc slots")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.tri, (size_t)(3 * (g.nt ? g.nt : 1)), "triangle slots")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.tri_n, (size_t)(g.nt ? g.nt : 1), "triangle slots")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.leaf_ref, (size_t)np, "leaf references")) != RTG_OK) break;
@@ -686,8 +685,8 @@ int build_lbvh(rtg_context* ctx) {
     if ((rc = dalloc(ctx, g.parent, (size_t)(2 * np), "LBVH parents")) != RTG_OK) break;
     // slots first: the Karras kernel reads the leaf references
     slots_kernel<<<blocks_for(np, 256), 256, 0, st>>>(vals.p, rank.p, np, g.nd, g.disc_cr_by_id.p,
-                                                      g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc_cr.p,
-                                                      g.disc_n.p, g.tri.p, g.tri_n.p, g.leaf_ref.p,
+                                                      g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc.p,
+                                                      g.tri.p, g.tri_n.p, g.leaf_ref.p,
                                                       g.leaf_prim.p);
     if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "slots"); break; }
     if (np > 1) {

@@ -86,8 +86,7 @@ int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc) {
 SceneView scene_view(rtg_context* ctx) {
   const Geometry& g = ctx->g;
   SceneView s{};
-  s.disc_cr = g.disc_cr.p;
-  s.disc_n = g.disc_n.p;
+  s.disc = g.disc.p;
   s.nd = (int32_t)g.nd;
   s.tri = g.tri.p;
   s.tri_n = g.tri_n.p;
