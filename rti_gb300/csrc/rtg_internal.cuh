@@ -42,9 +42,8 @@ struct SceneView {
   // discs in LBVH (slot) order, 32 B each: (centre, radius), (normal, original id bits)
   const float4* disc;
   int32_t nd;
-  // triangles in slot order: v0 + original id bits, e1, e2 (3 float4 per slot)
+  // triangles in slot order, 64 B each: (v0, original id bits), e1, e2, unit normal
   const float4* tri;
-  const float4* tri_n;  // unit normal per slot
   int32_t nt;
   const Node* nodes;
   uint32_t root;        // child reference of the root (internal node 0 or a leaf)
@@ -110,7 +109,7 @@ struct Geometry {
   DBuf<uint32_t> tri_idx;  // nt*3
   // slot-ordered copies
   DBuf<float4> disc;       // 2 per slot: (centre, radius), (normal, id bits)
-  DBuf<float4> tri, tri_n;
+  DBuf<float4> tri;        // 4 per slot: (v0, id bits), e1, e2, unit normal
   DBuf<Node> nodes;
   DBuf<uint32_t> leaf_ref;    // per sorted leaf i: child reference
   DBuf<int32_t> leaf_prim;    // per sorted leaf i: original primitive id

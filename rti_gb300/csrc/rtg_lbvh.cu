@@ -117,7 +117,7 @@ __global__ void slots_kernel(const uint32_t* __restrict__ sorted_prim, const uin
                              int64_t np, int64_t nd, const float4* __restrict__ dcr_id,
                              const float4* __restrict__ dn_id, const float4* __restrict__ tv,
                              const uint32_t* __restrict__ tidx, float4* __restrict__ disc,
-                             float4* __restrict__ tri, float4* __restrict__ tri_n,
+                             float4* __restrict__ tri,
                              uint32_t* __restrict__ leaf_ref, int32_t* __restrict__ leaf_prim) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= np) return;
@@ -138,10 +138,10 @@ __global__ void slots_kernel(const uint32_t* __restrict__ sorted_prim, const uin
     f3 e2 = sub3(mk3(c.x, c.y, c.z), v0);
     // util::compute_normal + normalize (i_triangle_reader.hpp:22-38)
     f3 n = normalize3(cross3(e1, e2));
-    tri[3 * ts] = make_float4(v0.x, v0.y, v0.z, __int_as_float((int)p));
-    tri[3 * ts + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
-    tri[3 * ts + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
-    tri_n[ts] = make_float4(n.x, n.y, n.z, 0.0f);
+    tri[4 * (int64_t)ts] = make_float4(v0.x, v0.y, v0.z, __int_as_float((int)p));
+    tri[4 * (int64_t)ts + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+    tri[4 * (int64_t)ts + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+    tri[4 * (int64_t)ts + 3] = make_float4(n.x, n.y, n.z, 0.0f);
     leaf_ref[i] = kLeafBit | kTriBit | ts;
   }
 }
@@ -342,7 +342,7 @@ __device__ __forceinline__ void child_box(uint32_t ref, const float4* __restrict
                                           float* hi) {
   if (ref & kLeafBit) {
     uint32_t slot = ref & kSlotMask;
-    int p = (ref & kTriBit) ? __float_as_int(tri[3 * slot].w) : __float_as_int(dn[2 * (int64_t)slot + 1].w);
+    int p = (ref & kTriBit) ? __float_as_int(tri[4 * (int64_t)slot].w) : __float_as_int(dn[2 * (int64_t)slot + 1].w);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       lo[a] = plo[3 * (int64_t)p + a];
@@ -614,7 +614,7 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
   if (d_sorted_prim) {
     slots_kernel<<<blocks_for(np, 256), 256, 0, st>>>(d_sorted_prim, d_disc_rank, np, g.nd, g.disc_cr_by_id.p,
                                                       g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc.p,
-                                                      g.tri.p, g.tri_n.p, g.leaf_ref.p,
+                                                      g.tri.p, g.leaf_ref.p,
                                                       g.leaf_prim.p);
     RTG_CUDA(ctx, cudaGetLastError());
   }
@@ -676,8 +676,7 @@ int build_lbvh(rtg_context* ctx) {
     disc_flag_kernel<<<blocks_for(np, 256), 256, 0, st>>>(vals.p, np, g.nd, rank.p);
     if ((rc = exclusive_scan_u32(ctx, rank.p, np, nullptr, st)) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.disc, (size_t)(2 * (g.nd ? g.nd : 1)), "disc slots")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, g.tri, (size_t)(3 * (g.nt ? g.nt : 1)), "triangle slots")) != RTG_OK) break;
-    if ((rc = dalloc(ctx, g.tri_n, (size_t)(g.nt ? g.nt : 1), "triangle slots")) != RTG_OK) break;
+    if ((rc = dalloc(ctx, g.tri, (size_t)(4 * (g.nt ? g.nt : 1)), "triangle slots")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.leaf_ref, (size_t)np, "leaf references")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.leaf_prim, (size_t)np, "leaf primitives")) != RTG_OK) break;
     const int64_t nn = np > 1 ? np - 1 : 1;
@@ -686,7 +685,7 @@ int build_lbvh(rtg_context* ctx) {
     // slots first: the Karras kernel reads the leaf references
     slots_kernel<<<blocks_for(np, 256), 256, 0, st>>>(vals.p, rank.p, np, g.nd, g.disc_cr_by_id.p,
                                                       g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc.p,
-                                                      g.tri.p, g.tri_n.p, g.leaf_ref.p,
+                                                      g.tri.p, g.leaf_ref.p,
                                                       g.leaf_prim.p);
     if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "slots"); break; }
     if (np > 1) {

@@ -67,9 +67,11 @@ __device__ __forceinline__ void test_leaf(const SceneView& s, uint32_t ref, cons
   int id;
   bool h;
   if (ref & kTriBit) {
-    const float4 a = __ldg(&s.tri[3 * slot]);
-    const float4 b = __ldg(&s.tri[3 * slot + 1]);
-    const float4 c = __ldg(&s.tri[3 * slot + 2]);
+    float4 a, b;  // (v0, id bits), e1 as one 256-bit load; e2 as one 128-bit load
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(s.tri + 4 * (int64_t)slot));
+    const float4 c = __ldg(&s.tri[4 * (int64_t)slot + 2]);
     id = __float_as_int(a.w);
     h = tri_test(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), r.o, r.d, tnear, t);
   } else {
@@ -387,7 +389,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
     const int axis = boundary_exit(*pp, o, d, tb);
     if (hit && (axis < 0 || th <= tb)) {
       float4 nn;
-      if (href & kTriBit) nn = __ldg(&pp->s.tri_n[href & kSlotMask]);
+      if (href & kTriBit) nn = __ldg(&pp->s.tri[4 * (int64_t)(href & kSlotMask) + 3]);
       else nn = __ldg(&pp->s.disc[2 * (int64_t)(href & kSlotMask) + 1]);
       const f3 n = mk3(nn.x, nn.y, nn.z);
       const f3 hp = mk3(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);

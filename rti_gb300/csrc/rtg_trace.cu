@@ -89,7 +89,6 @@ SceneView scene_view(rtg_context* ctx) {
   s.disc = g.disc.p;
   s.nd = (int32_t)g.nd;
   s.tri = g.tri.p;
-  s.tri_n = g.tri_n.p;
   s.nt = (int32_t)g.nt;
   s.nodes = g.nodes.p;
   s.root = g.root;

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(TPB) wf_shade_kernel(const TraceParams* __rest
     const int axis = boundary_exit(*pp, o, d, tb);
     if (hid >= 0 && (axis < 0 || th <= tb)) {
       float4 nn;
-      if (href & kTriBit) nn = __ldg(&pp->s.tri_n[href & kSlotMask]);
+      if (href & kTriBit) nn = __ldg(&pp->s.tri[4 * (int64_t)(href & kSlotMask) + 3]);
       else nn = __ldg(&pp->s.disc[2 * (int64_t)(href & kSlotMask) + 1]);
       const f3 nv = mk3(nn.x, nn.y, nn.z);
       const f3 hp = mk3(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
