@@ -318,7 +318,7 @@ int rtg_destroy(rtg_context* ctx) {
   dfree(g.disc_cr_by_id); dfree(g.disc_n_by_id); dfree(g.tri_v); dfree(g.tri_idx);
   dfree(g.disc); dfree(g.tri); dfree(g.nodes);
   dfree(g.leaf_ref); dfree(g.leaf_prim); dfree(g.parent); dfree(g.prim_lo); dfree(g.prim_hi);
-  dfree(g.refit_flags); dfree(g.nb_ptr); dfree(g.nb_idx);
+  dfree(g.refit_flags); dfree(g.nb_ptr); dfree(g.nb_idx); dfree(g.nb_slot); dfree(g.disc_slot);
   dfree(ctx->sticking_field); dfree(ctx->acc); dfree(ctx->cnt); dfree(ctx->areas); dfree(ctx->est);
   dfree(ctx->stat_tmp);
   free_wavefront(ctx->wf);

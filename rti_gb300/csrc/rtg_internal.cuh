@@ -47,11 +47,10 @@ struct SceneView {
   int32_t nt;
   const Node* nodes;
   uint32_t root;        // child reference of the root (internal node 0 or a leaf)
-  // neighbour CSR over original disc ids, and disc data by original id
+  // neighbour CSR: rows by original disc id, columns as disc slots (the
+  // neighbour's record in `disc` carries its original id)
   const int64_t* nb_ptr;
-  const int32_t* nb_idx;
-  const float4* disc_cr_by_id;
-  const float4* disc_n_by_id;
+  const uint32_t* nb_slot;
   const float* sticking_field;  // by original id or nullptr
 };
 
@@ -119,7 +118,9 @@ struct Geometry {
   uint32_t root = 0;
   // neighbours
   DBuf<int64_t> nb_ptr;
-  DBuf<int32_t> nb_idx;
+  DBuf<int32_t> nb_idx;       // columns as original ids
+  DBuf<uint32_t> nb_slot;     // the same columns as disc slots (read by the trace)
+  DBuf<uint32_t> disc_slot;   // by original disc id: its slot
   int64_t nb_nnz = 0;
   // centre extents and max radius (rti's box rule)
   float cmin[3] = {0, 0, 0}, cmax[3] = {0, 0, 0};

@@ -117,7 +117,7 @@ __global__ void slots_kernel(const uint32_t* __restrict__ sorted_prim, const uin
                              int64_t np, int64_t nd, const float4* __restrict__ dcr_id,
                              const float4* __restrict__ dn_id, const float4* __restrict__ tv,
                              const uint32_t* __restrict__ tidx, float4* __restrict__ disc,
-                             float4* __restrict__ tri,
+                             uint32_t* __restrict__ disc_slot, float4* __restrict__ tri,
                              uint32_t* __restrict__ leaf_ref, int32_t* __restrict__ leaf_prim) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= np) return;
@@ -127,6 +127,7 @@ __global__ void slots_kernel(const uint32_t* __restrict__ sorted_prim, const uin
   if (p < (uint32_t)nd) {
     float4 n = dn_id[p];
     disc[2 * (int64_t)ds] = dcr_id[p];
+    disc_slot[p] = ds;
     disc[2 * (int64_t)ds + 1] = make_float4(n.x, n.y, n.z, __int_as_float((int)p));
     leaf_ref[i] = kLeafBit | ds;
   } else {
@@ -614,7 +615,7 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
   if (d_sorted_prim) {
     slots_kernel<<<blocks_for(np, 256), 256, 0, st>>>(d_sorted_prim, d_disc_rank, np, g.nd, g.disc_cr_by_id.p,
                                                       g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc.p,
-                                                      g.tri.p, g.leaf_ref.p,
+                                                      g.disc_slot.p, g.tri.p, g.leaf_ref.p,
                                                       g.leaf_prim.p);
     RTG_CUDA(ctx, cudaGetLastError());
   }
@@ -676,6 +677,7 @@ int build_lbvh(rtg_context* ctx) {
     disc_flag_kernel<<<blocks_for(np, 256), 256, 0, st>>>(vals.p, np, g.nd, rank.p);
     if ((rc = exclusive_scan_u32(ctx, rank.p, np, nullptr, st)) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.disc, (size_t)(2 * (g.nd ? g.nd : 1)), "disc slots")) != RTG_OK) break;
+    if ((rc = dalloc(ctx, g.disc_slot, (size_t)(g.nd ? g.nd : 1), "disc slot map")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.tri, (size_t)(4 * (g.nt ? g.nt : 1)), "triangle slots")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.leaf_ref, (size_t)np, "leaf references")) != RTG_OK) break;
     if ((rc = dalloc(ctx, g.leaf_prim, (size_t)np, "leaf primitives")) != RTG_OK) break;
@@ -685,7 +687,7 @@ int build_lbvh(rtg_context* ctx) {
     // slots first: the Karras kernel reads the leaf references
     slots_kernel<<<blocks_for(np, 256), 256, 0, st>>>(vals.p, rank.p, np, g.nd, g.disc_cr_by_id.p,
                                                       g.disc_n_by_id.p, g.tri_v.p, g.tri_idx.p, g.disc.p,
-                                                      g.tri.p, g.leaf_ref.p,
+                                                      g.disc_slot.p, g.tri.p, g.leaf_ref.p,
                                                       g.leaf_prim.p);
     if (cudaGetLastError() != cudaSuccess) { rc = check_cuda(ctx, cudaGetLastError(), "slots"); break; }
     if (np > 1) {

@@ -407,9 +407,11 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
       if (!(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
         const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
         for (int64_t q = q0; q < q1; ++q) {
-          const int nb = __ldg(&pp->s.nb_idx[q]);
-          const float4 cr = __ldg(&pp->s.disc_cr_by_id[nb]);
-          const float4 nv = __ldg(&pp->s.disc_n_by_id[nb]);
+          float4 cr, nv;  // the neighbour's slot record: (centre, radius), (normal, id bits)
+          asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+              : "=f"(cr.x), "=f"(cr.y), "=f"(cr.z), "=f"(cr.w), "=f"(nv.x), "=f"(nv.y), "=f"(nv.z), "=f"(nv.w)
+              : "l"(pp->s.disc + 2 * (int64_t)__ldg(&pp->s.nb_slot[q])));
+          const int nb = __float_as_int(nv.w);
           if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
             if (M == kModeForward) deposit(*pp, nb, v);
             else G += __ldg(&pp->adj_g[nb]);

@@ -344,6 +344,13 @@ __global__ void stats_kernel(const double* __restrict__ s1, const double* __rest
 
 }  // namespace
 
+// Neighbour columns as disc slots, for the trace (one 256-bit record load per neighbour).
+__global__ void nb_slot_kernel(const int32_t* __restrict__ nb_idx, int64_t nnz, const uint32_t* __restrict__ slot_of_id,
+                               uint32_t* __restrict__ nb_slot) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nnz) nb_slot[q] = slot_of_id[nb_idx[q]];
+}
+
 int build_neighbors(rtg_context* ctx) {
   Geometry& g = ctx->g;
   cudaStream_t st = ctx->stream;
@@ -354,6 +361,7 @@ int build_neighbors(rtg_context* ctx) {
   if (nd == 1) {
     RTG_CUDA(ctx, cudaMemsetAsync(g.nb_ptr.p, 0, 2 * sizeof(int64_t), st));
     RTG_TRY(dalloc(ctx, g.nb_idx, 1, "neighbour columns"));
+    RTG_TRY(dalloc(ctx, g.nb_slot, 1, "neighbour slots"));
     return RTG_OK;
   }
   Grid grid;
@@ -406,6 +414,9 @@ int build_neighbors(rtg_context* ctx) {
     if ((rc = dalloc(ctx, g.nb_idx, (size_t)(nnz > 0 ? nnz : 1), "neighbour columns")) != RTG_OK) break;
     neighbor_kernel<true><<<blocks_for(nd, 128), 128, 0, st>>>(g.disc_cr_by_id.p, nd, grid, vals.p, cs.p, ce.p,
                                                                nullptr, g.nb_ptr.p, g.nb_idx.p);
+    if ((rc = dalloc(ctx, g.nb_slot, (size_t)(nnz > 0 ? nnz : 1), "neighbour slots")) != RTG_OK) break;
+    if (nnz > 0)
+      nb_slot_kernel<<<blocks_for(nnz, 256), 256, 0, st>>>(g.nb_idx.p, nnz, g.disc_slot.p, g.nb_slot.p);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) rc = check_cuda(ctx, e, "neighbour lists");

@@ -93,9 +93,7 @@ SceneView scene_view(rtg_context* ctx) {
   s.nodes = g.nodes.p;
   s.root = g.root;
   s.nb_ptr = g.nd > 0 ? g.nb_ptr.p : nullptr;
-  s.nb_idx = g.nb_idx.p;
-  s.disc_cr_by_id = g.disc_cr_by_id.p;
-  s.disc_n_by_id = g.disc_n_by_id.p;
+  s.nb_slot = g.nb_slot.p;
   s.sticking_field = ctx->sticking_field.p;
   return s;
 }

@@ -159,9 +159,12 @@ __global__ void __launch_bounds__(TPB) wf_shade_kernel(const TraceParams* __rest
         if (!(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
           const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
           for (int64_t q = q0; q < q1; ++q) {
-            const int nb = __ldg(&pp->s.nb_idx[q]);
-            const float4 cr = __ldg(&pp->s.disc_cr_by_id[nb]);
-            const float4 nb_n = __ldg(&pp->s.disc_n_by_id[nb]);
+            float4 cr, nb_n;  // the neighbour's slot record
+            asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                : "=f"(cr.x), "=f"(cr.y), "=f"(cr.z), "=f"(cr.w), "=f"(nb_n.x), "=f"(nb_n.y), "=f"(nb_n.z),
+                  "=f"(nb_n.w)
+                : "l"(pp->s.disc + 2 * (int64_t)__ldg(&pp->s.nb_slot[q])));
+            const int nb = __float_as_int(nb_n.w);
             if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nb_n.x, nb_n.y, nb_n.z))) {
               deposit(*pp, nb, v);
               c_tot += 1;
