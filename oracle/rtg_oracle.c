@@ -726,10 +726,22 @@ static void trace_path(const orc_scene* s, const orc_config* cf, uint64_t id, ac
  *  unbiased (1): adds the likelihood ratio of each roulette survival
  *    (probability w/0.3), which extends T to the whole path total L_p:
  *      dL/ds_j = sum over deposits k on j of G_k w_k - (L_p - P_k)/(1 - s_j).
- * A sticking field replays each stretch (held) or the whole path (unbiased)
- * twice from a snapshot of its start: first for T, then to scatter.  Both:
+ * With a sticking field each deposit's term is split as G_k w_k + P_k/(1 - s_j),
+ * added at the deposit, minus T/(1 - s_j), added at the end of the stretch
+ * (the whole path for the unbiased estimator) from a list of the stretch's
+ * (element, sticking) pairs of at most ORC_ADJ_LIST entries; a longer stretch
+ * is traced again from a snapshot of its start to add them -- the same split
+ * and the same replay decisions as the GPU kernel.  Both:
  *   dL/dn = sum over paths of (1/(n+1) + ln cos theta_0) L_p. */
 typedef struct { double ds, dn; double* field; } adj_acc_t;
+
+#define ORC_ADJ_LIST 32
+
+/* the deferred terms -T/(1 - s_j) of a stretch whose deposits all fit the list */
+static void adj_flush(adj_acc_t* a, const int32_t* id, const float* st, int n, double t) {
+  for (int i = 0; i < n; ++i)
+    if (st[i] < 1.0f) a->field[id[i]] += -t / (1.0 - (double)st[i]);
+}
 
 static void adjoint_path(const orc_scene* s, const orc_config* cf, uint64_t id, const double* g, int unbiased,
                          adj_acc_t* a, uint64_t* segs) {
@@ -740,11 +752,14 @@ static void adjoint_path(const orc_scene* s, const orc_config* cf, uint64_t id, 
   float w = 1.0f;
   uint32_t k = 0, nseg = 0;
   const double score = 1.0 / ((double)cf->source_exponent + 1.0) + log(-(double)d.z);
-  double wd = 0.0, lp = 0.0, seg_t = 0.0, seg_p = 0.0, pa = 0.0, psum = 0.0, ncoll = 0.0;
+  double wd = 0.0, lp = 0.0, seg_t = 0.0, pa = 0.0, psum = 0.0, ncoll = 0.0;
   int sub = 0;
   v3 so = o, sd = d;
   float sw = w;
   uint32_t sk = k, snseg = nseg;
+  int32_t list_id[ORC_ADJ_LIST];
+  float list_s[ORC_ADJ_LIST];
+  int list_n = 0;
   const double lower = cf->roulette_threshold * 1.0f, renew = cf->roulette_weight * 1.0f;
   const float s_glob = cf->sticking;
   for (;;) {
@@ -786,13 +801,18 @@ static void adjoint_path(const orc_scene* s, const orc_config* cf, uint64_t id, 
             wd -= dv;
           }
         } else if (sub == 0) {
-          seg_t += gv;
-        } else {
-          seg_p += gv;
+          seg_t += gv; /* P_k */
           lp += gv;
-          double gr = G * (double)w;
-          if (st < 1.0f) gr -= (seg_t - seg_p) / (1.0 - (double)st);
-          a->field[p] += gr;
+          double ak = G * (double)w;
+          if (st < 1.0f) ak += seg_t / (1.0 - (double)st);
+          a->field[p] += ak;
+          if (list_n < ORC_ADJ_LIST) {
+            list_id[list_n] = p;
+            list_s[list_n] = st;
+          }
+          list_n += 1;
+        } else if (st < 1.0f) { /* replay of a long stretch: seg_t holds its total */
+          a->field[p] += -seg_t / (1.0 - (double)st);
         }
         w = w - v;
         if (w == 0.0f) {
@@ -817,12 +837,13 @@ static void adjoint_path(const orc_scene* s, const orc_config* cf, uint64_t id, 
             o = hp;
             k += 1;
             if (fieldmode && reset && !unbiased) {
-              if (sub == 0) {
+              if (sub == 0 && list_n > ORC_ADJ_LIST) {
                 o = so; d = sd; w = sw; k = sk; nseg = snseg;
-                seg_p = 0.0; sub = 1;
+                sub = 1;
               } else {
+                if (sub == 0) adj_flush(a, list_id, list_s, list_n, seg_t);
                 so = o; sd = d; sw = w; sk = k; snseg = nseg;
-                seg_t = 0.0; seg_p = 0.0; sub = 0;
+                seg_t = 0.0; sub = 0; list_n = 0;
               }
             }
             continue;
@@ -846,9 +867,13 @@ static void adjoint_path(const orc_scene* s, const orc_config* cf, uint64_t id, 
     }
     if (ended) {
       if (fieldmode && sub == 0) {
-        o = so; d = sd; w = sw; k = sk; nseg = snseg;
-        seg_p = 0.0; sub = 1;
-        continue;
+        if (list_n <= ORC_ADJ_LIST) {
+          adj_flush(a, list_id, list_s, list_n, seg_t);
+        } else {
+          o = so; d = sd; w = sw; k = sk; nseg = snseg;
+          sub = 1;
+          continue;
+        }
       }
       if (!fieldmode && unbiased) {
         double ds = pa;

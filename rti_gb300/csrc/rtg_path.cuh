@@ -260,9 +260,13 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 //   unbiased (adj_unbiased = 1): adds the likelihood ratio of each roulette
 //     survival (probability w/0.3); T becomes the path total L_p.  One global
 //     s: dL/ds = sum_k G_k w_k - (K L_p - sum_k P_k)/(1 - s) over K deposits.
-//   kModeAdjField traces each stretch (held) or the whole path (unbiased)
-//     twice from a snapshot of its start: first for T, then to scatter the
-//     gradients; no per-path memory is kept.
+//   kModeAdjField splits each deposit's term as G_k w_k + P_k/(1 - s_j) (known
+//     at the deposit, scattered at once) minus T/(1 - s_j) (T known at the end
+//     of the stretch -- the whole path for the unbiased estimator).  The
+//     deferred part is scattered from a small per-lane list of the stretch's
+//     (element, sticking) pairs; a stretch with more deposits than the list
+//     holds is traced again from a snapshot of its start to scatter them, so
+//     no per-path memory is kept.
 //   Both: dL/dn = sum over paths of (1/(n+1) + ln cos theta_0) * L_p (score
 //     function of the cos^n source).
 // Batched = true: lanes take global ray ids over the concatenated ray ranges
@@ -285,23 +289,37 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
   uint32_t k = 0, nseg = 0;
   const uint64_t nrays = Batched ? prefix[njobs] : p0.ray_end - p0.ray_begin;
   // adjoint state
-  double wd = 0.0, lp = 0.0, score = 0.0, acc_s = 0.0, acc_n = 0.0, seg_t = 0.0, seg_p = 0.0;
+  double wd = 0.0, lp = 0.0, score = 0.0, acc_s = 0.0, acc_n = 0.0, seg_t = 0.0;
   double pa = 0.0, psum = 0.0, ncoll = 0.0;
   const bool unbiased = p0.adj_unbiased != 0;
   int sub = 0;
   f3 so = o, sd = d;
   float sw = 1.0f;
   uint32_t sk = 0, snseg = 0;
+  constexpr int kAdjList = 32;  // deposits of a stretch whose deferred term is kept per lane
+  uint32_t alist_id[M == kModeAdjField ? kAdjList : 1];
+  float alist_s[M == kModeAdjField ? kAdjList : 1];
+  int alist_n = 0;
   auto snapshot = [&]() {
     so = o; sd = d; sw = w; sk = k; snseg = nseg;
-    seg_t = 0.0; seg_p = 0.0; sub = 0;
+    seg_t = 0.0; sub = 0; alist_n = 0;
   };
-  // end of a path; in the field replay the first pass of a stretch restarts it
+  // the deferred terms -T/(1 - s_j) of a stretch whose deposits all fit the list
+  auto flush = [&]() {
+    for (int i = 0; i < alist_n; ++i)
+      if (alist_s[i] < 1.0f) atomicAdd(&pp->adj_field[alist_id[i]], -seg_t / (1.0 - (double)alist_s[i]));
+  };
+  // end of a path; in the field replay a stretch too long for the list is
+  // traced again to scatter its deferred terms
   auto path_end = [&]() -> bool {
     if (M == kModeAdjField && sub == 0) {
-      o = so; d = sd; w = sw; k = sk; nseg = snseg;
-      seg_p = 0.0; sub = 1;
-      return true;
+      if (alist_n <= kAdjList) {
+        flush();
+      } else {
+        o = so; d = sd; w = sw; k = sk; nseg = snseg;
+        sub = 1;
+        return true;
+      }
     }
     if (M == kModeAdjGlobal && unbiased) {
       double ds = pa;
@@ -434,13 +452,18 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
       } else if (M == kModeAdjField) {
         const double gv = G * (double)v;
         if (sub == 0) {
-          seg_t += gv;
-        } else {
-          seg_p += gv;
+          seg_t += gv;  // P_k
           lp += gv;
-          double gr = G * (double)w;
-          if (st < 1.0f) gr -= (seg_t - seg_p) / (1.0 - (double)st);
-          atomicAdd(&pp->adj_field[hid], gr);
+          double a = G * (double)w;
+          if (st < 1.0f) a += seg_t / (1.0 - (double)st);
+          atomicAdd(&pp->adj_field[hid], a);
+          if (alist_n < kAdjList) {
+            alist_id[alist_n] = (uint32_t)hid;
+            alist_s[alist_n] = st;
+          }
+          alist_n += 1;
+        } else if (st < 1.0f) {  // replay of a long stretch: seg_t holds its total T
+          atomicAdd(&pp->adj_field[hid], -seg_t / (1.0 - (double)st));
         }
       }
       w = w - v;
@@ -470,10 +493,11 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
       o = hp;
       k += 1;
       if (M == kModeAdjField && reset && !unbiased) {
-        if (sub == 0) {  // the stretch is complete: trace it again to scatter
+        if (sub == 0 && alist_n > kAdjList) {  // the stretch is complete: trace it again to scatter
           o = so; d = sd; w = sw; k = sk; nseg = snseg;
-          seg_p = 0.0; sub = 1;
+          sub = 1;
         } else {
+          if (sub == 0) flush();
           snapshot();  // the next stretch starts after this re-emission
         }
       }
