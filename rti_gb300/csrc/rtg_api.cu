@@ -507,8 +507,8 @@ int rtg_set_tree_builder(rtg_context* ctx, int32_t builder) {
   ctx->g.builder = builder;
   if (ctx->g.nd + ctx->g.nt > 0 && ctx->g.nodes.p && builder != keep) {
     RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    const int rc = build_lbvh(ctx);
-    if (rc != RTG_OK) return rc;
+    RTG_TRY(build_lbvh(ctx));
+    RTG_TRY(build_neighbors(ctx));  // neighbour columns are stored as slots of the new tree
     ctx->traced = false;
     ctx->finalized = false;
   }
