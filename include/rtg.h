@@ -184,6 +184,25 @@ RTG_API int rtg_get_tree_depth(const rtg_context* ctx, int32_t* depth);
 #define RTG_TREE_PLOC 1
 RTG_API int rtg_set_tree_builder(rtg_context* ctx, int32_t builder);
 RTG_API int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder);
+/* What a front-face disc hit deposits.  rti has two treatments of
+ * overlapping discs:
+ *   RTG_DEPOSIT_NEIGHBORS (default): w*s on the hit disc and on every
+ *     overlapping neighbour disc the ray crosses, then w -= w*s -- rti's
+ *     tracer (tracer.hpp:229-240,339-383);
+ *   RTG_DEPOSIT_WINDOW: the multi-hit window of rti's point-cloud context
+ *     (trace/point_cloud_context.hpp:132-173,265-286): the window opens at the
+ *     closest front-face disc hit t0 (rti: whichever hit Embree's filter
+ *     reports first) and reaches to t0 + window_factor * r0 (r0 that disc's
+ *     radius; rti: 5), closed earlier by the first back-face disc hit beyond
+ *     t0 or by the x/y box; every disc hit from the front within it receives
+ *     w*s_j (s_j its own sticking), and w drops by the mean of those deposits.
+ *     Forward traces of one context only: rtg_adjoint and rtg_batch_add
+ *     refuse a context in this mode.  Triangles deposit on the hit triangle.
+ * Applies to later traces; window_factor >= 0 is used by RTG_DEPOSIT_WINDOW. */
+#define RTG_DEPOSIT_NEIGHBORS 0
+#define RTG_DEPOSIT_WINDOW 1
+RTG_API int rtg_set_deposit_mode(rtg_context* ctx, int32_t mode, float window_factor);
+RTG_API int rtg_get_deposit_mode(const rtg_context* ctx, int32_t* mode, float* window_factor);
 /* Autotuner: for each tree builder (RTG_TREE_*), times each candidate launch
  * configuration (block size x packet x stack depth x scheduling) on source
  * rays [0, sample_rays) with `seed` under the current surface and

@@ -43,6 +43,8 @@ class OrcConfig(C.Structure):
         ("job", C.c_uint32),
         ("seed", C.c_uint64),
         ("sticking_field", _f32p),
+        ("window", C.c_int32),
+        ("window_factor", C.c_float),
     ]
 
 
@@ -136,6 +138,14 @@ def local_intersect(org, dir_, disc, normal) -> bool:
     c = np.ascontiguousarray(disc, dtype=np.float32)
     n = np.ascontiguousarray(normal, dtype=np.float32)
     return bool(lib().orc_local_intersect(_p(o, _f32p), _p(d, _f32p), _p(c, _f32p), _p(n, _f32p)))
+
+
+def source_ray(cfg: OrcConfig, ray_id: int):
+    """(origin, direction) of source ray `ray_id` under cfg."""
+    o = np.zeros(3, dtype=np.float32)
+    d = np.zeros(3, dtype=np.float32)
+    lib().orc_source_ray(C.byref(cfg), C.c_uint64(ray_id), _p(o, _f32p), _p(d, _f32p))
+    return o, d
 
 
 def diffuse_dir(normal, u_phi: int, u_t: int):
@@ -253,7 +263,7 @@ def adjoint(scene: "Scene", cfg: OrcConfig, g, ray_begin: int, ray_end: int, nth
 
 def make_config(box_lo, box_hi, *, x_bound=1, y_bound=1, reflection=0, specular_fraction=0.0,
                 sticking=0.1, source_exponent=1.0, tnear=1e-4, max_segments=1 << 16, job=0, seed=0,
-                src_lo=None, src_hi=None) -> OrcConfig:
+                src_lo=None, src_hi=None, window=0, window_factor=5.0) -> OrcConfig:
     c = OrcConfig()
     c.x_bound, c.y_bound, c.reflection = x_bound, y_bound, reflection
     c.specular_fraction, c.sticking, c.source_exponent = specular_fraction, sticking, source_exponent
@@ -269,6 +279,7 @@ def make_config(box_lo, box_hi, *, x_bound=1, y_bound=1, reflection=0, specular_
     c.roulette_threshold, c.roulette_weight = 0.1, 0.3
     c.max_segments, c.job, c.seed = max_segments, job, seed
     c.sticking_field = None
+    c.window, c.window_factor = window, window_factor
     return c
 
 

@@ -637,6 +637,69 @@ static inline void acc_use(acc_t* a, int32_t p, float v) {
   a->t.total += 1;
 }
 
+/* The multi-hit window of rti's point-cloud context (point_cloud_context.hpp:
+ * 132-173 filter, 265-286 post-processing), restated with a defined order:
+ * the window opens at the closest front-face hit t0, on disc p0, instead of at
+ * whichever hit Embree's filter reports first.  It reaches to
+ * t0 + window_factor * r0 (rti: 5 radii of the first disc, :163), cut at the
+ * x/y box exit tbox (rti's boundary hit is accepted and ends the query) and at
+ * the first back-face disc hit or triangle hit beyond t0 (rti accepts a
+ * back-face hit once the window is open, :145-153).  Every disc hit from the
+ * front within it receives w s_j (each disc once, :271-281); w then drops by
+ * the mean of those deposits (:283-285).  Scans the BVH for every primitive
+ * hit in [0, te]; returns the new weight. */
+static float window_deposit(const orc_scene* s, const orc_config* cf, v3 o, v3 d, float t0, float tbox, int32_t p0,
+                            float w, acc_t* a) {
+  float te = t0 + cf->window_factor * s->dc[4 * p0 + 3];
+  if (tbox < te) te = tbox;
+  const v3 idr = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+  float tc = te;
+  double sum = 0.0;
+  uint64_t n = 0;
+  for (int pass = 0; pass < 2; ++pass) { /* 0: where the window closes; 1: the deposits */
+    int32_t stack[256];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+      const bnode* nd = &s->nodes[stack[--sp]];
+      if (!box_hit(nd, o, idr, tc)) continue;
+      if (!nd->count) {
+        if (sp + 2 <= 256) {
+          stack[sp++] = nd->right;
+          stack[sp++] = nd->left;
+        }
+        continue;
+      }
+      for (int32_t k = nd->left; k < nd->left + nd->count; ++k) {
+        const int32_t p = s->order[k];
+        float t;
+        int h, closes;
+        if (p < s->nd) {
+          const v3 nrm = disc_n(s, p);
+          h = disc_test(disc_c(s, p), s->dc[4 * p + 3], nrm, o, d, cf->tnear, &t);
+          closes = d.x * nrm.x + d.y * nrm.y + d.z * nrm.z > 0.0f;
+        } else {
+          const int64_t q = p - s->nd;
+          h = tri_test(ld3(s->tv0, q), ld3(s->te1, q), ld3(s->te2, q), o, d, cf->tnear, &t);
+          closes = 1;
+        }
+        if (!h) continue;
+        if (pass == 0) {
+          if (closes && t > t0 && t < tc) tc = t;
+        } else if (p < s->nd && !closes && t >= t0 && t <= tc) {
+          const float st = cf->sticking_field ? cf->sticking_field[p] : cf->sticking;
+          const float v = w * st;
+          acc_use(a, p, v);
+          sum += (double)v;
+          n += 1;
+        }
+      }
+    }
+  }
+  if (n > 1) a->t.nb_deposits += n - 1;
+  return n > 0 ? (float)((double)w - sum / (double)n) : w;
+}
+
 /* One path of tracer::run (tracer.hpp:160-280). */
 static void trace_path(const orc_scene* s, const orc_config* cf, uint64_t id, acc_t* a) {
   float w = 1.0f;
@@ -665,17 +728,21 @@ static void trace_path(const orc_scene* s, const orc_config* cf, uint64_t id, ac
       a->t.hitc += 1;
       float st = cf->sticking_field ? cf->sticking_field[p] : cf->sticking;
       float v = w * st;
-      acc_use(a, p, v);
-      if (p < s->nd && s->nb_ptr) {
-        for (int64_t q = s->nb_ptr[p]; q < s->nb_ptr[p + 1]; ++q) {
-          int32_t nb = s->nb_idx[q];
-          if (local_intersect(o, d, disc_c(s, nb), s->dc[4 * nb + 3], disc_n(s, nb))) {
-            acc_use(a, nb, v);
-            a->t.nb_deposits += 1;
+      if (cf->window && p < s->nd) {
+        w = window_deposit(s, cf, o, d, th, axis >= 0 ? tb : FLT_MAX, p, w, a);
+      } else {
+        acc_use(a, p, v);
+        if (p < s->nd && s->nb_ptr) {
+          for (int64_t q = s->nb_ptr[p]; q < s->nb_ptr[p + 1]; ++q) {
+            int32_t nb = s->nb_idx[q];
+            if (local_intersect(o, d, disc_c(s, nb), s->dc[4 * nb + 3], disc_n(s, nb))) {
+              acc_use(a, nb, v);
+              a->t.nb_deposits += 1;
+            }
           }
         }
+        w = w - v;
       }
-      w = w - v;
       if (w == 0.0f) break;
       uint32_t u[4];
       draw4(cf->seed, id, k, cf->job, u);
@@ -890,6 +957,7 @@ int orc_adjoint(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e
                 int unbiased, double* field_grad, double* scalars, uint64_t* segments) {
   int64_t np = s->np;
   if (cf->sticking_field && !field_grad) return 1;
+  if (cf->window) return 1; /* the adjoint replays the neighbour deposit only */
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #else

@@ -42,6 +42,8 @@ typedef struct orc_config {
   uint32_t job;                /* Philox stream tag (instance/species) */
   uint64_t seed;
   const float* sticking_field; /* per-primitive sticking, or NULL */
+  int32_t  window;             /* 1: multi-hit window deposit (point_cloud_context.hpp) */
+  float    window_factor;      /* window length in radii of the disc that opens it (rti: 5) */
 } orc_config;
 
 typedef struct orc_tally {

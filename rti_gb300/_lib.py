@@ -44,6 +44,7 @@ EXPORTS = [
     "rtg_get_tree_depth", "rtg_autotune", "rtg_batch_set_launch_config", "rtg_batch_get_launch_config",
     "rtg_batch_autotune", "rtg_write_vtp", "rtg_write_vtp_discs", "rtg_write_vtp_triangles", "rtg_write_vtp_mixed",
     "rtg_read_point_cloud", "rtg_read_triangles", "rtg_set_tree_builder", "rtg_get_tree_builder",
+    "rtg_set_deposit_mode", "rtg_get_deposit_mode",
 ]
 
 RTG_ADJ_HELD = 0
@@ -55,6 +56,8 @@ RTG_TREE_KARRAS = 0
 RTG_LEAF_IMMEDIATE = 0
 RTG_LEAF_POSTPONED = 1
 RTG_TREE_PLOC = 1
+RTG_DEPOSIT_NEIGHBORS = 0
+RTG_DEPOSIT_WINDOW = 1
 
 
 class RtgConfig(C.Structure):
@@ -190,6 +193,8 @@ def load(path: str | None = None):
         "rtg_read_triangles": (C.c_int, [C.c_char_p, _i64p, _f32p, _i64p, _u32p, C.c_char_p, C.c_int32]),
         "rtg_set_tree_builder": (C.c_int, [_ctx, C.c_int32]),
         "rtg_get_tree_builder": (C.c_int, [_ctx, _i32p]),
+        "rtg_set_deposit_mode": (C.c_int, [_ctx, C.c_int32, C.c_float]),
+        "rtg_get_deposit_mode": (C.c_int, [_ctx, _i32p, _f32p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

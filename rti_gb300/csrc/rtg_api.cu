@@ -224,6 +224,8 @@ int prepare_trace_with(rtg_context* ctx, const rtg_config& c, const float* box_l
   p.max_segments = c.max_segments;
   p.job = c.job;
   p.adj_inv_n1 = 1.0 / ((double)c.source_exponent + 1.0);
+  p.window = ctx->deposit_mode == RTG_DEPOSIT_WINDOW ? 1 : 0;
+  p.window_factor = ctx->window_factor;
   return RTG_OK;
 }
 
@@ -521,6 +523,24 @@ int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder) {
   return RTG_OK;
 }
 
+int rtg_set_deposit_mode(rtg_context* ctx, int32_t mode, float window_factor) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (mode != RTG_DEPOSIT_NEIGHBORS && mode != RTG_DEPOSIT_WINDOW)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "mode must be RTG_DEPOSIT_NEIGHBORS or RTG_DEPOSIT_WINDOW");
+  if (!(window_factor >= 0.0f && window_factor < 1e30f))
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "window_factor must be finite and >= 0");
+  ctx->deposit_mode = mode;
+  ctx->window_factor = window_factor;
+  return RTG_OK;
+}
+
+int rtg_get_deposit_mode(const rtg_context* ctx, int32_t* mode, float* window_factor) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (mode) *mode = ctx->deposit_mode;
+  if (window_factor) *window_factor = ctx->window_factor;
+  return RTG_OK;
+}
+
 int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
                  double* best_rays_per_s) {
   if (!ctx || sample_rays == 0) return RTG_ERR_INVALID_ARGUMENT;
@@ -647,6 +667,8 @@ int rtg_adjoint(rtg_context* ctx, const double* d_g, uint64_t ray_begin, uint64_
   const bool field = ctx->sticking_field.p != nullptr;
   if (field && !d_field_grad)
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a sticking field is set: d_field_grad is required");
+  if (ctx->deposit_mode != RTG_DEPOSIT_NEIGHBORS)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "the adjoint replays the neighbour deposit only");
   TraceParams p{};
   RTG_TRY(prepare_trace(ctx, ray_begin, ray_end, seed, p));
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;

@@ -79,6 +79,8 @@ struct TraceParams {
   uint32_t job;
   int32_t packet;  // a warp takes new source rays when at least this many lanes are idle
   int32_t plain;   // 1: one source ray per thread, no refill (grid covers all rays)
+  int32_t window;         // 1: multi-hit window deposit (RTG_DEPOSIT_WINDOW), traced by kModeWindow
+  float window_factor;    // window length in radii of the disc that opens it
   // adjoint replay (unused by the forward trace)
   const double* adj_g;     // dL/dS1 by primitive id
   double* adj_field;       // dL/ds_j by primitive id (sticking-field mode) or nullptr
@@ -92,6 +94,7 @@ struct TraceParams {
 constexpr int kModeForward = 0;
 constexpr int kModeAdjGlobal = 1;  // dL/ds (one global sticking) and dL/dn
 constexpr int kModeAdjField = 2;   // dL/ds_j (sticking field) and dL/dn
+constexpr int kModeWindow = 3;     // forward trace with the multi-hit window deposit
 
 // ---- device buffers owned by a context ----
 template <typename T>
@@ -169,6 +172,8 @@ struct rtg_context {
   bool finalized = false;
   float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
   rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL, RTG_LEAF_IMMEDIATE};
+  int32_t deposit_mode = RTG_DEPOSIT_NEIGHBORS;
+  float window_factor = 5.0f;  // point_cloud_context.hpp:163
   rtg::Wavefront wf;
   std::string err;
 };

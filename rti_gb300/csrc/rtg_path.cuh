@@ -206,6 +206,132 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   return bid != INT_MAX;
 }
 
+// hit_accumulator::use (hit_accumulator.hpp:128-138)
+__device__ __forceinline__ void deposit(const TraceParams& p, int id, float v) {
+  const double dv = (double)v;
+  atomicAdd(&p.s1[id], dv);
+  atomicAdd(&p.s2[id], dv * v);
+  atomicAdd(&p.s3[id], dv * v * v);
+  atomicAdd(&p.s4[id], dv * v * v * v);
+  atomicAdd(&p.cnt[id], 1ull);
+}
+
+// Does the ray overlap the box within [tlo, thi]?  Padded like slab(), so a
+// primitive hit in the interval is never outside an overlapping box.
+__device__ __forceinline__ bool overlaps(float lx, float hx, float ly, float hy, float lz, float hz, const Ray& r,
+                                         float tlo, float thi) {
+  float t0x = (lx - r.o.x) * r.idr.x, t1x = (hx - r.o.x) * r.idr.x;
+  float t0y = (ly - r.o.y) * r.idr.y, t1y = (hy - r.o.y) * r.idr.y;
+  float t0z = (lz - r.o.z) * r.idr.z, t1z = (hz - r.o.z) * r.idr.z;
+  const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
+  const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z)) * 1.0000005f;
+  return tn <= tf && tn <= thi * 1.0000005f + 1e-30f && tf >= tlo;
+}
+
+// Calls visit(ref) once for every leaf whose box the ray overlaps within
+// [tlo, thi].  errs counts stack overflows and iteration-limit trips.
+template <int STACK, typename Visit>
+__device__ void leaves_in_interval(const SceneView& s, const Ray& r, float tlo, float thi, unsigned long long& errs,
+                                   Visit visit) {
+  uint32_t stack[STACK];
+  int sp = 0;
+  uint32_t cur = s.root;
+  const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
+  for (int64_t it = 0;; ++it) {
+    if (it > max_iter) {
+      errs += 1;
+      return;
+    }
+    float4 a, b, c;
+    uint4 ch;
+    load_node(s.nodes + cur, a, b, c, ch);
+    bool h0 = overlaps(a.x, a.y, b.x, b.y, c.x, c.y, r, tlo, thi);
+    // a one-primitive tree holds its leaf in both children of the root
+    bool h1 = ch.y != ch.x && overlaps(a.z, a.w, b.z, b.w, c.z, c.w, r, tlo, thi);
+    if (h0 && (ch.x & kLeafBit)) {
+      visit(ch.x);
+      h0 = false;
+    }
+    if (h1 && (ch.y & kLeafBit)) {
+      visit(ch.y);
+      h1 = false;
+    }
+    if (h0 && h1) {
+      if (sp < STACK) stack[sp++] = ch.y;
+      else errs += 1;
+      cur = ch.x;
+    } else if (h0) {
+      cur = ch.x;
+    } else if (h1) {
+      cur = ch.y;
+    } else {
+      if (sp == 0) return;
+      cur = stack[--sp];
+    }
+  }
+}
+
+// The multi-hit window of rti's point-cloud context (point_cloud_context.hpp:
+// 132-173,265-286), opened by the closest front-face hit at t0 on the disc in
+// slot `ref`: it reaches to t0 + window_factor * r0 (r0 that disc's radius),
+// cut at the x/y box exit tbox and at the first back-face disc hit or triangle
+// hit beyond t0.  Every disc hit from the front within it receives w s_j; the
+// return value is w minus the mean of those deposits (float w, double mean,
+// as rti).  The sum of the deposits is formed in double; it is exact, hence
+// independent of the traversal order, while the deposits of one window lie
+// within a factor 2^28 of each other (always for a global sticking).
+template <int STACK>
+__device__ float window_deposit(const TraceParams& p, f3 o, f3 d, float t0, float tbox, uint32_t ref, float w,
+                                unsigned long long& c_tot, unsigned long long& c_nb, unsigned long long& errs) {
+  Ray r;
+  r.o = o;
+  r.d = d;
+  r.idr = mk3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+  const float r0 = __ldg(&p.s.disc[2 * (int64_t)(ref & kSlotMask)]).w;
+  float te = t0 + p.window_factor * r0;
+  if (tbox < te) te = tbox;
+  // hit of the leaf primitive in slot lr: t, id, and whether it closes the window
+  auto leaf = [&](uint32_t lr, float& t, int& id, bool& closes) -> bool {
+    const uint32_t slot = lr & kSlotMask;
+    if (lr & kTriBit) {
+      const float4 a = __ldg(&p.s.tri[4 * (int64_t)slot]), b = __ldg(&p.s.tri[4 * (int64_t)slot + 1]);
+      const float4 c = __ldg(&p.s.tri[4 * (int64_t)slot + 2]);
+      id = __float_as_int(a.w);
+      closes = true;
+      return tri_test(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), r.o, r.d, p.tnear, t);
+    }
+    const float4 cr = __ldg(&p.s.disc[2 * (int64_t)slot]), nn = __ldg(&p.s.disc[2 * (int64_t)slot + 1]);
+    id = __float_as_int(nn.w);
+    closes = d.x * nn.x + d.y * nn.y + d.z * nn.z > 0.0f;
+    return disc_test(mk3(cr.x, cr.y, cr.z), cr.w, mk3(nn.x, nn.y, nn.z), r.o, r.d, p.tnear, t);
+  };
+  float tc = te;
+  leaves_in_interval<STACK>(p.s, r, t0, te, errs, [&](uint32_t lr) {
+    float t;
+    int id;
+    bool closes;
+    if (leaf(lr, t, id, closes) && closes && t > t0 && t < tc) tc = t;
+  });
+  double sum = 0.0;
+  unsigned long long n = 0;
+  leaves_in_interval<STACK>(p.s, r, t0, tc, errs, [&](uint32_t lr) {
+    if (lr & kTriBit) return;
+    float t;
+    int id;
+    bool closes;
+    if (leaf(lr, t, id, closes) && !closes && t >= t0 && t <= tc) {
+      const float st = p.s.sticking_field ? __ldg(&p.s.sticking_field[id]) : p.sticking;
+      const float v = w * st;
+      deposit(p, id, v);
+      sum += (double)v;
+      n += 1;
+    }
+  });
+  c_tot += n;
+  c_nb += n > 0 ? n - 1 : 0;
+  return n > 0 ? (float)((double)w - sum / (double)n) : w;
+}
+
 // Side-face exit of the x/y box: 0 = x face, 1 = y face, -1 = the ray leaves
 // through the top or bottom first (a miss).
 __device__ __forceinline__ int boundary_exit(const TraceParams& p, f3 o, f3 d, float& tb) {
@@ -223,16 +349,6 @@ __device__ __forceinline__ int boundary_exit(const TraceParams& p, f3 o, f3 d, f
   if (t > tz) return -1;
   tb = t;
   return axis;
-}
-
-// hit_accumulator::use (hit_accumulator.hpp:128-138)
-__device__ __forceinline__ void deposit(const TraceParams& p, int id, float v) {
-  const double dv = (double)v;
-  atomicAdd(&p.s1[id], dv);
-  atomicAdd(&p.s2[id], dv * v);
-  atomicAdd(&p.s3[id], dv * v * v);
-  atomicAdd(&p.s4[id], dv * v * v * v);
-  atomicAdd(&p.cnt[id], 1ull);
 }
 
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
@@ -278,6 +394,7 @@ template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false>
 __global__ void __launch_bounds__(TPB, 1024 / TPB)
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
+  constexpr bool kAdj = M == kModeAdjGlobal || M == kModeAdjField;
   const TraceParams* pp = &p0;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -326,7 +443,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
       if (pp->sticking < 1.0f) ds -= (ncoll * lp - psum) / (1.0 - (double)pp->sticking);
       acc_s += ds;
     }
-    if (M != kModeForward) acc_n += score * lp;
+    if (kAdj) acc_n += score * lp;
     return false;
   };
   for (uint32_t iter = 0;; ++iter) {
@@ -368,7 +485,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
             k = 0;
             nseg = 0;
             active = true;
-            if (M != kModeForward) {
+            if (kAdj) {
               score = pp->adj_inv_n1 + log(-(double)d.z);
               lp = 0.0;
               wd = 0.0;
@@ -419,10 +536,15 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
       const float st = pp->s.sticking_field ? __ldg(&pp->s.sticking_field[hid]) : pp->sticking;
       const float v = w * st;
       double G = 0.0;
-      if (M == kModeForward) deposit(*pp, hid, v);
-      else G = __ldg(&pp->adj_g[hid]);
-      c_tot += 1;
-      if (!(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
+      float w_win = 0.0f;
+      if (M == kModeWindow && !(href & kTriBit)) {
+        w_win = window_deposit<STACK>(*pp, o, d, th, axis >= 0 ? tb : FLT_MAX, href, w, c_tot, c_nb, c_err);
+      } else {
+        if (kAdj) G = __ldg(&pp->adj_g[hid]);
+        else deposit(*pp, hid, v);
+        c_tot += 1;
+      }
+      if (M != kModeWindow && !(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
         const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
         for (int64_t q = q0; q < q1; ++q) {
           float4 cr, nv;  // the neighbour's slot record: (centre, radius), (normal, id bits)
@@ -431,8 +553,8 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
               : "l"(pp->s.disc + 2 * (int64_t)__ldg(&pp->s.nb_slot[q])));
           const int nb = __float_as_int(nv.w);
           if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
-            if (M == kModeForward) deposit(*pp, nb, v);
-            else G += __ldg(&pp->adj_g[nb]);
+            if (kAdj) G += __ldg(&pp->adj_g[nb]);
+            else deposit(*pp, nb, v);
             c_tot += 1;
             c_nb += 1;
           }
@@ -466,7 +588,8 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
           atomicAdd(&pp->adj_field[hid], -seg_t / (1.0 - (double)st));
         }
       }
-      w = w - v;
+      if (M == kModeWindow && !(href & kTriBit)) w = w_win;
+      else w = w - v;
       if (w == 0.0f) {
         active = path_end();
         continue;
@@ -519,7 +642,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
     c_non += 1;
     active = path_end();
   }
-  if (M != kModeForward) {
+  if (kAdj) {
     acc_s = warp_sum_d(acc_s);
     acc_n = warp_sum_d(acc_n);
     if (lane == 0) {

@@ -52,6 +52,11 @@ PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, int& tpb_out
     return stack <= 64 ? trace_paths_kernel<kModeAdjField, false, 128, 64>
                        : trace_paths_kernel<kModeAdjField, false, 128, 256>;
   }
+  if (mode == kModeWindow) {
+    tpb_out = 128;
+    return stack <= 64 ? trace_paths_kernel<kModeWindow, false, 128, 64>
+                       : trace_paths_kernel<kModeWindow, false, 128, 256>;
+  }
   tpb_out = tpb;
   if (tpb == 64) return forward_kernel<64>(stack, postpone);
   if (tpb == 256) return forward_kernel<256>(stack, postpone);
@@ -104,6 +109,8 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
   TraceParams p = p_in;
   p.packet = lc.packet;
   const uint64_t nrays = p.ray_end - p.ray_begin;
+  // the window deposit has a kernel of its own (megakernel or plain schedule)
+  if (mode == kModeForward && p.window) mode = kModeWindow;
   if (mode == kModeForward && lc.scheduling == RTG_SCHED_WAVEFRONT) {
     // a job table of one entry
     Wavefront& wf = ctx->wf;
@@ -117,7 +124,7 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
   }
   int tpb = 128, sms = 0, per_sm = 0;
   PathKernel kern = pick_kernel(mode, lc.threads_per_block, stack, lc.leaf_tests == RTG_LEAF_POSTPONED, tpb);
-  p.plain = mode == kModeForward && lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
+  p.plain = (mode == kModeForward || mode == kModeWindow) && lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));
   if (per_sm < 1) per_sm = 1;

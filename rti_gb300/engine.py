@@ -184,6 +184,18 @@ class Engine:
         """L.RTG_TREE_KARRAS (fast build) or L.RTG_TREE_PLOC (clustering); rebuilds the current tree."""
         self._check(self._L.rtg_set_tree_builder(self._h, int(builder)))
 
+    @property
+    def deposit_mode(self):
+        """(mode, window_factor): L.RTG_DEPOSIT_NEIGHBORS (rti's tracer) or
+        L.RTG_DEPOSIT_WINDOW (rti's multi-hit window of window_factor radii)."""
+        m, f = C.c_int32(), C.c_float()
+        self._check(self._L.rtg_get_deposit_mode(self._h, C.byref(m), C.byref(f)))
+        return m.value, f.value
+
+    def set_deposit_mode(self, mode: int, window_factor: float = 5.0):
+        """Selects the deposit of a front-face disc hit for later traces."""
+        self._check(self._L.rtg_set_deposit_mode(self._h, int(mode), float(window_factor)))
+
     def autotune(self, sample_rays: int, seed: int = 0):
         """Times the candidate launch configurations on a sample trace and keeps
         the fastest; returns (config dict, rays/s of the sample)."""
