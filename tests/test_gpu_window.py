@@ -46,7 +46,7 @@ def test_window_trench_matches_oracle(eng, oracle_lib, bound):
     s = oracle_lib.Scene(t.xyzr, t.normals)
     c = s.trace(oracle_lib.make_config(t.box_lo, t.box_hi, sticking=0.1, x_bound=bound, y_bound=bound, seed=7,
                                        window=1, window_factor=5.0), 0, n)
-    assert c.nb_deposits > c.hitc  # overlapping coplanar discs: several per window
+    assert c.nb_deposits > c.hitc // 4  # overlapping coplanar discs: several per window
     _compare(eng, c)
 
 
