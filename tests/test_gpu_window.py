@@ -54,7 +54,7 @@ def test_window_rough_sticking_field_matches_oracle(eng, oracle_lib):
     r = scenes.rough_discs(n=96, spacing=0.01, rms=0.02, corr=0.1, seed=3)
     field = np.random.default_rng(1).uniform(0.05, 0.6, r.n).astype(np.float32)
     eng.upload_discs(r.points, r.normals, r.radii)
-    eng.configure(box=(r.box_lo, r.box_hi), reflection=2, specular_fraction=0.3, reset=True)
+    eng.configure(box=(r.box_lo, r.box_hi), reflection=2, specular_fraction=0.3, x_bound=1, y_bound=1, reset=True)
     eng.set_sticking_field(field)
     eng.set_deposit_mode(1, 2.5)
     n = 100000
