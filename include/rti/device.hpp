@@ -209,6 +209,10 @@ class device final {
   void set(ray::i_direction<numeric_type>& srcDirection) { exponent = srcDirection.rtg_exponent(); }
   void set_seed(uint64_t s) { seed = s; }
   void set_cuda_device(int d) { cuda_device = d; }
+  // rti's other treatment of overlapping discs, the multi-hit window of
+  // trace/point_cloud_context.hpp (rti: 5 radii), instead of its tracer's
+  // neighbour deposit; radii < 0 selects the neighbour deposit again.
+  void set_multi_hit_window(numeric_type radii = 5) { window = radii; }
 
   void run() {
     if (points.size() != spacing.size() || points.size() != normals.size())
@@ -232,6 +236,7 @@ class device final {
     std::unique_ptr<rtg_context, int (*)(rtg_context*)> ctx(raw, rtg_destroy);
     check(rtg_upload_discs(raw, &points[0][0], &normals[0][0], spacing.data(), (int64_t)n), raw, "upload");
     check(rtg_set_config(raw, &cfg), raw, "configuration");
+    if (window >= 0) check(rtg_set_deposit_mode(raw, RTG_DEPOSIT_WINDOW, (float)window), raw, "deposit mode");
     if (!field.empty()) check(rtg_set_sticking_field(raw, field.data(), (int64_t)n), raw, "sticking");
     check(rtg_trace(raw, (uint64_t)numofrays, seed, nullptr), raw, "trace");
     mcestimates.assign(n, 0.0f);
@@ -315,6 +320,7 @@ class device final {
   bound_condition xCond = bound_condition::REFLECTIVE;
   bound_condition yCond = bound_condition::REFLECTIVE;
   numeric_type exponent = 1;
+  numeric_type window = -1;  // < 0: neighbour deposit
   uint64_t seed = 0;
   int cuda_device = 0;
 };

@@ -106,6 +106,7 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    '                                 rti::rng::i_rng&, rti::rng::i_rng::i_state&) override { return 0.1f; }\n'
                    '  void init_new() override {}\n};\n'
                    'int main() { rti::device<float, p, rti::reflection::diffuse<float>> d; d.set_number_of_rays(10);'
+                   ' d.set_multi_hit_window(5.0f);'
                    ' return 0; }\n')
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
                        capture_output=True, text=True)

@@ -5,7 +5,8 @@ A small C++ program uses rti::device<float, particle, reflection> exactly as
 rti's users do (set_points / set_normals / set_grid_spacing / set_x / set_y /
 set_number_of_rays / run / get_mc_estimates / get_hit_cnts), for a particle
 whose sticking comes from get_sticking_probability(), one with a constant
-`rtg_sticking`, and one with get_sticking_field()."""
+`rtg_sticking`, one with get_sticking_field(), and the constant one with the
+multi-hit window deposit (set_multi_hit_window)."""
 import os
 import subprocess
 
@@ -47,7 +48,7 @@ std::vector<T> load(const std::string& path, size_t n) {
 }
 
 template <typename P, typename R>
-void run(const std::string& dir, const std::string& tag, size_t n) {
+void run(const std::string& dir, const std::string& tag, size_t n, bool window = false) {
   auto pts = load<std::array<float, 3>>(dir + "/points.bin", n);
   auto nrm = load<std::array<float, 3>>(dir + "/normals.bin", n);
   auto rad = load<float>(dir + "/radii.bin", n);
@@ -58,6 +59,7 @@ void run(const std::string& dir, const std::string& tag, size_t n) {
   d.set_x(rti::geo::bound_condition::PERIODIC);
   d.set_y(rti::geo::bound_condition::PERIODIC);
   d.set_number_of_rays(200000);
+  if (window) d.set_multi_hit_window(5.0f);
   d.run();
   auto est = d.get_mc_estimates();
   auto cnt = d.get_hit_cnts();
@@ -78,6 +80,7 @@ int main(int argc, char** argv) {
   run<per_disc, rti::reflection::diffuse<float>>(dir, "per_disc", n);
   run<constant, rti::reflection::mixed<float, 10>>(dir, "constant", n);
   run<field, rti::reflection::specular<float>>(dir, "field", n);
+  run<constant, rti::reflection::diffuse<float>>(dir, "window", n, true);
   std::printf("ok\n");
   return 0;
 }
@@ -111,10 +114,22 @@ def test_cpp_dropin_matches_binding(rtg_lib, tmp_path):
         return device_run(t.points, t.normals, t.radii, n_rays=200000, seed=0, config=c,
                           sticking_field=sticking_field)
 
+    def expect_window():
+        from rti_gb300 import Engine
+        e = Engine(0)
+        e.upload_discs(t.points, t.normals, t.radii)
+        e.configure(x_bound=L.RTG_BOUND_PERIODIC, y_bound=L.RTG_BOUND_PERIODIC, sticking=0.1, reset=True)
+        e.set_deposit_mode(L.RTG_DEPOSIT_WINDOW, 5.0)
+        e.trace(200000, 0)
+        out = e.mc_estimates(), e.hit_counts()
+        e.close()
+        return out
+
     ids = np.arange(n)
     cases = {"per_disc": expect(np.where(ids % 2 == 1, 0.1, 0.3).astype(np.float32), L.RTG_REFLECT_DIFFUSE, 0.0),
              "constant": expect(None, L.RTG_REFLECT_MIXED, np.float32(0.1)),
-             "field": expect(np.full(n, 0.25, np.float32), L.RTG_REFLECT_SPECULAR, 1.0)}
+             "field": expect(np.full(n, 0.25, np.float32), L.RTG_REFLECT_SPECULAR, 1.0),
+             "window": expect_window()}
     for tag, (est, cnt) in cases.items():
         est_cpp = np.fromfile(tmp_path / f"{tag}_est.bin", dtype=np.float32)
         cnt_cpp = np.fromfile(tmp_path / f"{tag}_cnt.bin", dtype=np.uint64)
