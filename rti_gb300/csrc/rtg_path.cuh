@@ -28,6 +28,7 @@ namespace rtg {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr uint32_t kNoLeaf = 0xFFFFFFFFu;  // no child reference: slots stay below kSlotMask
 
 __device__ __forceinline__ float safe_inv(float d) {
   if (fabsf(d) < 1e-30f) d = d < 0.0f ? -1e-30f : 1e-30f;
@@ -123,14 +124,19 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
       float tn0, tn1;
       bool h0 = slab(a.x, a.y, b.x, b.y, c.x, c.y, r, bt, tn0);
       bool h1 = slab(a.z, a.w, b.z, b.w, c.z, c.w, r, bt, tn1);
-      if (h0 && (ch.x & kLeafBit)) {
-        test_leaf(s, ch.x, r, tnear, bt, bid, bref);
-        h0 = false;
+      // The leaf children go through one code path, so the lanes with a leaf
+      // at child 0 and those with one at child 1 test together (a warp runs
+      // the test once per node step, twice only where a lane has two leaves).
+      const bool l0 = h0 && (ch.x & kLeafBit), l1 = h1 && (ch.y & kLeafBit);
+      uint32_t lf = l0 ? ch.x : (l1 ? ch.y : kNoLeaf);
+      uint32_t lf2 = l0 && l1 ? ch.y : kNoLeaf;
+      while (lf != kNoLeaf) {
+        test_leaf(s, lf, r, tnear, bt, bid, bref);
+        lf = lf2;
+        lf2 = kNoLeaf;
       }
-      if (h1 && (ch.y & kLeafBit)) {
-        test_leaf(s, ch.y, r, tnear, bt, bid, bref);
-        h1 = false;
-      }
+      h0 = h0 && !l0;
+      h1 = h1 && !l1;
       if (h0 && h1) {
         uint32_t nearc = tn0 <= tn1 ? ch.x : ch.y;
         uint32_t farc = tn0 <= tn1 ? ch.y : ch.x;
