@@ -56,6 +56,9 @@ RTG_TREE_KARRAS = 0
 RTG_LEAF_IMMEDIATE = 0
 RTG_LEAF_POSTPONED = 1
 RTG_TREE_PLOC = 1
+RTG_STACK_AUTO = 0
+RTG_STACK_LOCAL = 1
+RTG_STACK_SHARED = 2
 RTG_DEPOSIT_NEIGHBORS = 0
 RTG_DEPOSIT_WINDOW = 1
 
@@ -92,7 +95,7 @@ class RtgDeviceView(C.Structure):
 
 class RtgLaunchConfig(C.Structure):
     _fields_ = [("threads_per_block", C.c_int32), ("packet", C.c_int32), ("stack_depth", C.c_int32),
-                ("scheduling", C.c_int32), ("leaf_tests", C.c_int32)]
+                ("scheduling", C.c_int32), ("leaf_tests", C.c_int32), ("stack_memory", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

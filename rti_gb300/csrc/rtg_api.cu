@@ -479,6 +479,7 @@ void rtg_launch_config_default(rtg_launch_config* lc) {
   lc->stack_depth = 0;
   lc->scheduling = RTG_SCHED_MEGAKERNEL;
   lc->leaf_tests = RTG_LEAF_IMMEDIATE;
+  lc->stack_memory = RTG_STACK_AUTO;
 }
 
 int rtg_set_launch_config(rtg_context* ctx, const rtg_launch_config* lc) {
@@ -601,6 +602,19 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
         rc = run(cand[order[q]].lc, ms);
         if (rc == RTG_OK && ms < cand[order[q]].ms) cand[order[q]].ms = ms;
       }
+    // the three fastest with their stacks in the other memory, best of two
+    for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
+      Cand alt = cand[order[q]];
+      if (alt.lc.scheduling == RTG_SCHED_WAVEFRONT) continue;
+      alt.lc.stack_memory = shared_stack(ctx, alt.lc) ? RTG_STACK_LOCAL : RTG_STACK_SHARED;
+      float m2 = 0.0f;
+      rc = run(alt.lc, alt.ms);
+      if (rc == RTG_OK) rc = run(alt.lc, m2);
+      if (rc == RTG_OK) {
+        alt.ms = std::min(alt.ms, m2);
+        cand.push_back(alt);
+      }
+    }
   }
   ctx->traced = false;
   ctx->finalized = false;

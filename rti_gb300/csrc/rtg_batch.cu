@@ -379,6 +379,19 @@ int rtg_batch_autotune(rtg_batch* b, double fraction, rtg_launch_config* best, d
       rc = run(cand[order[q]], ms);
       if (rc == RTG_OK && ms < tms[order[q]]) tms[order[q]] = ms;
     }
+  // the three fastest with their stacks in shared memory, best of two
+  for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
+    rtg_launch_config alt = cand[order[q]];
+    if (alt.scheduling == RTG_SCHED_WAVEFRONT) continue;
+    alt.stack_memory = RTG_STACK_SHARED;
+    float m1 = 0.0f, m2 = 0.0f;
+    rc = run(alt, m1);
+    if (rc == RTG_OK) rc = run(alt, m2);
+    if (rc == RTG_OK) {
+      cand.push_back(alt);
+      tms.push_back(std::min(m1, m2));
+    }
+  }
   dfree(dp);
   if (rc != RTG_OK) {
     ctx->lc = keep;

@@ -200,6 +200,8 @@ int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float t
 SceneView scene_view(rtg_context* ctx);
 // stack entries for a requested depth (0 = automatic) and a tree depth: 32, 64 or 256
 int stack_for(int requested, int tree_depth);
+// whether a trace of ctx under lc keeps its traversal stacks in shared memory
+bool shared_stack(rtg_context* ctx, const rtg_launch_config& lc);
 int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc);
 // trace_batched.cu: the megakernel over a job table (forward only)
 int launch_trace_batched(rtg_context* ctx, const TraceParams& p0, const TraceParams* d_jobs, const uint64_t* d_prefix,

@@ -98,9 +98,12 @@ __device__ __forceinline__ void test_leaf(const SceneView& s, uint32_t ref, cons
 // lane of the warp holds a pending leaf (or has no inner node left), then the
 // warp tests the pending leaves together; the closest hit is the same, only
 // the lanes that run the primitive tests together change.
-template <int STACK, bool POSTPONE>
+// SST = 0: the stack is a per-thread local array; SST > 0: it is a column of
+// shared memory, entry i at sstk[i * SST] (SST = the block size, so the lanes
+// of a warp always hit distinct banks).
+template <int STACK, bool POSTPONE, int SST = 0>
 __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& bt, int& bid, uint32_t& bref,
-                            unsigned long long& errs) {
+                            unsigned long long& errs, uint32_t* sstk = nullptr) {
   Ray r;
   r.o = o;
   r.d = d;
@@ -108,7 +111,8 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   bt = FLT_MAX;
   bid = INT_MAX;
   bref = 0xFFFFFFFFu;
-  uint32_t stack[STACK];
+  uint32_t lstack[SST ? 1 : STACK];
+  auto stack = [&](int i) -> uint32_t& { return SST ? sstk[i * SST] : lstack[i]; };
   int sp = 0;
   uint32_t cur = s.root;
   const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
@@ -141,7 +145,7 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
         uint32_t nearc = tn0 <= tn1 ? ch.x : ch.y;
         uint32_t farc = tn0 <= tn1 ? ch.y : ch.x;
         if (sp < STACK) {
-          stack[sp++] = farc;
+          stack(sp++) = farc;
         } else {
           errs += 1;
         }
@@ -152,7 +156,7 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
         cur = ch.y;
       } else {
         if (sp == 0) break;
-        cur = stack[--sp];
+        cur = stack(--sp);
       }
     }
     return bid != INT_MAX;
@@ -161,7 +165,7 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   constexpr uint32_t kNone = 0xFFFFFFFFu;
   uint32_t leaf = kNone;
   int64_t it = 0;
-  auto pop = [&]() -> uint32_t { return sp > 0 ? stack[--sp] : kNone; };
+  auto pop = [&]() -> uint32_t { return sp > 0 ? stack(--sp) : kNone; };
   while (cur != kNone) {
     // inner nodes until every lane of the warp holds a pending leaf
     while (cur != kNone && !(cur & kLeafBit)) {
@@ -178,7 +182,7 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
       const bool h1 = slab(a.z, a.w, b.z, b.w, c.z, c.w, r, bt, tn1);
       if (h0 && h1) {
         const bool first = tn0 <= tn1;
-        if (sp < STACK) stack[sp++] = first ? ch.y : ch.x;
+        if (sp < STACK) stack(sp++) = first ? ch.y : ch.x;
         else errs += 1;
         cur = first ? ch.x : ch.y;
       } else if (h0) {
@@ -396,11 +400,20 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // its job's parameters (scene, configuration, accumulators); the counters and
 // the abort flag are the batch's (p0).  TPB threads per block and 1024 / TPB
 // resident blocks per SM as the register target (64 registers per thread).
-template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false>
+// SHSTACK = true: the traversal stacks of the block live in shared memory
+// (STACK x TPB entries, at most 32 KB).
+template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false, bool SHSTACK = false>
 __global__ void __launch_bounds__(TPB, 1024 / TPB)
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
   constexpr bool kAdj = M == kModeAdjGlobal || M == kModeAdjField;
+  static_assert(!SHSTACK || STACK * TPB * 4 <= 32768, "a shared stack of at most 32 KB per block");
+  constexpr int kSst = SHSTACK ? TPB : 0;
+  uint32_t* sstk = nullptr;
+  if constexpr (SHSTACK) {
+    __shared__ uint32_t sstack[STACK * TPB];
+    sstk = sstack + threadIdx.x;
+  }
   const TraceParams* pp = &p0;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -526,7 +539,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
     float th, tb = 0.0f;
     int hid;
     uint32_t href;
-    const bool hit = closest_hit<STACK, POSTPONE>(pp->s, o, d, pp->tnear, th, hid, href, c_err);
+    const bool hit = closest_hit<STACK, POSTPONE, kSst>(pp->s, o, d, pp->tnear, th, hid, href, c_err, sstk);
     const int axis = boundary_exit(*pp, o, d, tb);
     if (hit && (axis < 0 || th <= tb)) {
       float4 nn;
@@ -672,6 +685,18 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
     atomicAdd(&p0.tally->nb_deposits, c_nb);
     atomicAdd(&p0.tally->errors, c_err);
   }
+}
+
+using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_t*, int);
+
+// The instantiation of trace_paths_kernel with its stack in shared memory
+// when `shared` asks for it and it fits 32 KB per block, else in local memory.
+template <int M, bool Batched, int TPB, int STACK, bool POSTPONE>
+PathKernel kernel_for(bool shared) {
+  if constexpr (STACK * TPB * 4 <= 32768) {
+    if (shared) return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, true>;
+  }
+  return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, false>;
 }
 
 }  // namespace

@@ -26,30 +26,28 @@ __global__ void closest_hit_kernel(const SceneView s, const float* __restrict__ 
   if (e) atomicAdd(errors, e);
 }
 
-using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_t*, int);
-
 template <int TPB, bool POSTPONE>
-PathKernel forward_kernel(int stack) {
-  if (stack <= 32) return trace_paths_kernel<kModeForward, false, TPB, 32, POSTPONE>;
-  if (stack <= 64) return trace_paths_kernel<kModeForward, false, TPB, 64, POSTPONE>;
-  return trace_paths_kernel<kModeForward, false, TPB, 256, POSTPONE>;
+PathKernel forward_kernel(int stack, bool shared) {
+  if (stack <= 32) return kernel_for<kModeForward, false, TPB, 32, POSTPONE>(shared);
+  if (stack <= 64) return kernel_for<kModeForward, false, TPB, 64, POSTPONE>(shared);
+  return kernel_for<kModeForward, false, TPB, 256, POSTPONE>(shared);
 }
 
 template <int TPB>
-PathKernel forward_kernel(int stack, bool postpone) {
-  return postpone ? forward_kernel<TPB, true>(stack) : forward_kernel<TPB, false>(stack);
+PathKernel forward_kernel(int stack, bool postpone, bool shared) {
+  return postpone ? forward_kernel<TPB, true>(stack, shared) : forward_kernel<TPB, false>(stack, shared);
 }
 
 // The adjoint replays run with 128 threads and a 64- or 256-entry stack.
-PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, int& tpb_out) {
+PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, bool shared, int& tpb_out) {
   if (mode == kModeAdjGlobal) {
     tpb_out = 128;
-    return stack <= 64 ? trace_paths_kernel<kModeAdjGlobal, false, 128, 64>
+    return stack <= 64 ? kernel_for<kModeAdjGlobal, false, 128, 64, false>(shared)
                        : trace_paths_kernel<kModeAdjGlobal, false, 128, 256>;
   }
   if (mode == kModeAdjField) {
     tpb_out = 128;
-    return stack <= 64 ? trace_paths_kernel<kModeAdjField, false, 128, 64>
+    return stack <= 64 ? kernel_for<kModeAdjField, false, 128, 64, false>(shared)
                        : trace_paths_kernel<kModeAdjField, false, 128, 256>;
   }
   if (mode == kModeWindow) {
@@ -58,13 +56,23 @@ PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, int& tpb_out
                        : trace_paths_kernel<kModeWindow, false, 128, 256>;
   }
   tpb_out = tpb;
-  if (tpb == 64) return forward_kernel<64>(stack, postpone);
-  if (tpb == 256) return forward_kernel<256>(stack, postpone);
+  if (tpb == 64) return forward_kernel<64>(stack, postpone, shared);
+  if (tpb == 256) return forward_kernel<256>(stack, postpone, shared);
   tpb_out = 128;
-  return forward_kernel<128>(stack, postpone);
+  return forward_kernel<128>(stack, postpone, shared);
 }
 
 }  // namespace
+
+bool shared_stack(rtg_context* ctx, const rtg_launch_config& lc) {
+  if (lc.stack_memory == RTG_STACK_SHARED) return true;
+  if (lc.stack_memory == RTG_STACK_LOCAL) return false;
+  int l2 = 0;
+  if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device) != cudaSuccess) return false;
+  const Geometry& g = ctx->g;
+  const size_t bytes = g.nodes.n * sizeof(Node) + (g.disc.n + g.tri.n) * sizeof(float4);
+  return l2 > 0 && bytes > (size_t)l2;
+}
 
 int stack_for(int requested, int tree_depth) {
   const int need = requested > tree_depth ? requested : tree_depth;
@@ -85,6 +93,8 @@ int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc) {
     return bad("scheduling must be RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT or RTG_SCHED_PLAIN");
   if (lc.leaf_tests != RTG_LEAF_IMMEDIATE && lc.leaf_tests != RTG_LEAF_POSTPONED)
     return bad("leaf_tests must be RTG_LEAF_IMMEDIATE or RTG_LEAF_POSTPONED");
+  if (lc.stack_memory != RTG_STACK_AUTO && lc.stack_memory != RTG_STACK_LOCAL && lc.stack_memory != RTG_STACK_SHARED)
+    return bad("stack_memory must be RTG_STACK_AUTO, RTG_STACK_LOCAL or RTG_STACK_SHARED");
   return RTG_OK;
 }
 
@@ -123,7 +133,8 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
     return launch_wavefront(ctx, p, wf.one_job.p, wf.one_prefix.p, 1, nrays, st, lc, ctx->g.depth);
   }
   int tpb = 128, sms = 0, per_sm = 0;
-  PathKernel kern = pick_kernel(mode, lc.threads_per_block, stack, lc.leaf_tests == RTG_LEAF_POSTPONED, tpb);
+  PathKernel kern = pick_kernel(mode, lc.threads_per_block, stack, lc.leaf_tests == RTG_LEAF_POSTPONED,
+                                shared_stack(ctx, lc), tpb);
   p.plain = (mode == kModeForward || mode == kModeWindow) && lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));

@@ -6,18 +6,16 @@ namespace rtg {
 
 namespace {
 
-using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_t*, int);
-
 template <int TPB, bool POSTPONE>
-PathKernel batched_kernel(int stack) {
-  if (stack <= 32) return trace_paths_kernel<kModeForward, true, TPB, 32, POSTPONE>;
-  if (stack <= 64) return trace_paths_kernel<kModeForward, true, TPB, 64, POSTPONE>;
-  return trace_paths_kernel<kModeForward, true, TPB, 256, POSTPONE>;
+PathKernel batched_kernel(int stack, bool shared) {
+  if (stack <= 32) return kernel_for<kModeForward, true, TPB, 32, POSTPONE>(shared);
+  if (stack <= 64) return kernel_for<kModeForward, true, TPB, 64, POSTPONE>(shared);
+  return kernel_for<kModeForward, true, TPB, 256, POSTPONE>(shared);
 }
 
 template <int TPB>
-PathKernel batched_kernel(int stack, bool postpone) {
-  return postpone ? batched_kernel<TPB, true>(stack) : batched_kernel<TPB, false>(stack);
+PathKernel batched_kernel(int stack, bool postpone, bool shared) {
+  return postpone ? batched_kernel<TPB, true>(stack, shared) : batched_kernel<TPB, false>(stack, shared);
 }
 
 }  // namespace
@@ -33,8 +31,10 @@ int launch_trace_batched(rtg_context* ctx, const TraceParams& p0_in, const Trace
   p0.plain = lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
   int tpb = lc.threads_per_block, sms = 0, per_sm = 0;
   const bool pp = lc.leaf_tests == RTG_LEAF_POSTPONED;
-  PathKernel kern = tpb == 64 ? batched_kernel<64>(stack, pp) : tpb == 256 ? batched_kernel<256>(stack, pp)
-                                                                           : batched_kernel<128>(stack, pp);
+  const bool sh = lc.stack_memory == RTG_STACK_SHARED;  // AUTO: local (the jobs' trees differ in size)
+  PathKernel kern = tpb == 64    ? batched_kernel<64>(stack, pp, sh)
+                    : tpb == 256 ? batched_kernel<256>(stack, pp, sh)
+                                 : batched_kernel<128>(stack, pp, sh);
   if (tpb != 64 && tpb != 256) tpb = 128;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));

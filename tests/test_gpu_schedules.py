@@ -13,9 +13,12 @@ from rti_gb300 import scenes
 pytestmark = pytest.mark.gpu
 S1_RTOL = 1e-9
 MK, WF, PL = 0, 1, 2
+LOCAL, SHARED = 1, 2  # stack memory
 CONFIGS = [(64, 1, 0, MK), (256, 8, 0, MK), (128, 32, 256, MK), (128, 1, 32, MK), (128, 1, 0, WF),
            (256, 1, 256, WF), (64, 1, 64, WF), (128, 1, 0, PL), (256, 1, 64, PL),
-           (128, 1, 0, MK, 1), (256, 8, 256, MK, 1), (128, 1, 0, PL, 1)]
+           (128, 1, 0, MK, 1), (256, 8, 256, MK, 1), (128, 1, 0, PL, 1),
+           (128, 1, 0, MK, 0, SHARED), (64, 8, 64, MK, 1, SHARED), (256, 1, 0, PL, 0, SHARED),
+           (128, 1, 64, MK, 0, SHARED), (128, 1, 0, MK, 0, LOCAL), (256, 1, 256, MK, 0, SHARED)]
 
 
 @pytest.fixture(scope="module")
@@ -127,7 +130,8 @@ def test_batch_wavefront_and_autotune(rtg_lib):
         b.synchronize()
         ref = [b.results(j) for j in range(len(b))]
         t_ref = b.tally()
-        for cfg in [(128, 1, 0, WF), (64, 8, 256, MK), (256, 32, 0, MK), (128, 1, 0, PL), (128, 8, 0, MK, 1)]:
+        for cfg in [(128, 1, 0, WF), (64, 8, 256, MK), (256, 32, 0, MK), (128, 1, 0, PL), (128, 8, 0, MK, 1),
+                    (128, 1, 0, MK, 0, SHARED), (64, 8, 64, PL, 1, SHARED)]:
             b.set_launch_config(*cfg)
             b.run(use_graph=True)
             b.synchronize()
@@ -145,3 +149,22 @@ def test_batch_wavefront_and_autotune(rtg_lib):
             assert np.array_equal(b.results(j)[1], ref[j][1])
     for e in engines:
         e.close()
+
+
+def test_adjoint_with_the_stack_in_shared_memory(eng):
+    """The adjoint replays take the context's stack placement: same gradients."""
+    rng = np.random.default_rng(4)
+    _trench(eng)
+    g = rng.random(eng.num_primitives)
+    field_in = rng.uniform(0.05, 0.5, eng.num_primitives).astype(np.float32)
+    out = []
+    for mem in (LOCAL, SHARED):
+        eng.set_launch_config(stack_memory=mem)
+        ds, dn, _ = eng.adjoint(g, 50000, seed=2)
+        eng.set_sticking_field(field_in)
+        _, dn2, field = eng.adjoint(g, 50000, seed=2)
+        eng.set_sticking_field(None)
+        out.append((ds, dn, dn2, field))
+    eng.set_launch_config()
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12)
