@@ -123,7 +123,6 @@ typedef struct rtg_launch_config {
   int32_t scheduling;        /* RTG_SCHED_* */
   int32_t leaf_tests;        /* RTG_LEAF_*: when the primitives of a leaf the ray reaches are tested */
   int32_t stack_memory;      /* RTG_STACK_*: where the traversal stack of the path kernel lives */
-  int32_t ray_order;         /* RTG_ORDER_*: the order in which source rays start their paths */
 } rtg_launch_config;
 /* leaf_tests: on the spot, or postponed until every lane of the warp holds a
  * leaf (Aila and Laine's while-while traversal; megakernel and plain
@@ -140,15 +139,6 @@ typedef struct rtg_launch_config {
 #define RTG_STACK_AUTO 0
 #define RTG_STACK_LOCAL 1
 #define RTG_STACK_SHARED 2
-/* ray_order (megakernel forward traces of one context): RTG_ORDER_ID starts
- * the paths in ray-id order; RTG_ORDER_DEEP_FIRST first finds every source
- * ray's first hit (one closest-hit pass, whose results the paths then start
- * from) and starts the paths whose first hit lies deepest first: those are the
- * long ones in a cavity, and a long path started last is the tail of a trace.
- * Results are the same either way.  AUTO: deep first for 2^20 to 2^27 rays. */
-#define RTG_ORDER_AUTO 0
-#define RTG_ORDER_ID 1
-#define RTG_ORDER_DEEP_FIRST 2
 
 /* Fills *cfg with rti's defaults. */
 RTG_API void rtg_config_default(rtg_config* cfg);

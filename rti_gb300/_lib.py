@@ -59,9 +59,6 @@ RTG_TREE_PLOC = 1
 RTG_STACK_AUTO = 0
 RTG_STACK_LOCAL = 1
 RTG_STACK_SHARED = 2
-RTG_ORDER_AUTO = 0
-RTG_ORDER_ID = 1
-RTG_ORDER_DEEP_FIRST = 2
 RTG_DEPOSIT_NEIGHBORS = 0
 RTG_DEPOSIT_WINDOW = 1
 
@@ -98,8 +95,7 @@ class RtgDeviceView(C.Structure):
 
 class RtgLaunchConfig(C.Structure):
     _fields_ = [("threads_per_block", C.c_int32), ("packet", C.c_int32), ("stack_depth", C.c_int32),
-                ("scheduling", C.c_int32), ("leaf_tests", C.c_int32), ("stack_memory", C.c_int32),
-                ("ray_order", C.c_int32)]
+                ("scheduling", C.c_int32), ("leaf_tests", C.c_int32), ("stack_memory", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

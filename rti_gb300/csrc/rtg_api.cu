@@ -324,8 +324,6 @@ int rtg_destroy(rtg_context* ctx) {
   dfree(ctx->sticking_field); dfree(ctx->acc); dfree(ctx->cnt); dfree(ctx->areas); dfree(ctx->est);
   dfree(ctx->stat_tmp);
   free_wavefront(ctx->wf);
-  dfree(ctx->ro.order); dfree(ctx->ro.t); dfree(ctx->ro.id); dfree(ctx->ro.ref); dfree(ctx->ro.bucket);
-  dfree(ctx->ro.counts);
   if (ctx->d_tally) cudaFree(ctx->d_tally);
   if (ctx->d_tally_adj) cudaFree(ctx->d_tally_adj);
   if (ctx->h_abort) cudaFreeHost(ctx->h_abort);
@@ -482,7 +480,6 @@ void rtg_launch_config_default(rtg_launch_config* lc) {
   lc->scheduling = RTG_SCHED_MEGAKERNEL;
   lc->leaf_tests = RTG_LEAF_IMMEDIATE;
   lc->stack_memory = RTG_STACK_AUTO;
-  lc->ray_order = RTG_ORDER_AUTO;
 }
 
 int rtg_set_launch_config(rtg_context* ctx, const rtg_launch_config* lc) {

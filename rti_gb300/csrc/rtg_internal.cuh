@@ -81,13 +81,6 @@ struct TraceParams {
   int32_t plain;   // 1: one source ray per thread, no refill (grid covers all rays)
   int32_t window;         // 1: multi-hit window deposit (RTG_DEPOSIT_WINDOW), traced by kModeWindow
   float window_factor;    // window length in radii of the disc that opens it
-  // deep-first ray order (forward megakernel): local ray index of the j-th path
-  // to start, and the first closest hit of each local ray index (t, id, slot
-  // reference or kNoHit); order == nullptr: id order, every hit traced
-  const uint32_t* order;
-  const float* first_t;
-  const int32_t* first_id;
-  const uint32_t* first_ref;
   // adjoint replay (unused by the forward trace)
   const double* adj_g;     // dL/dS1 by primitive id
   double* adj_field;       // dL/ds_j by primitive id (sticking-field mode) or nullptr
@@ -141,19 +134,6 @@ struct Geometry {
 };
 
 // Wavefront scheduling state (device buffers, lazily allocated).
-// Scratch of the deep-first ray order: per local ray index its first closest
-// hit and depth bucket, the start order, and the bucket counters.
-struct RayOrder {
-  DBuf<uint32_t> order;
-  DBuf<float> t;
-  DBuf<int32_t> id;
-  DBuf<uint32_t> ref;
-  DBuf<uint8_t> bucket;
-  DBuf<unsigned int> counts;  // kOrderBuckets counts, then kOrderBuckets cursors
-};
-constexpr int kOrderBuckets = 32;
-constexpr uint32_t kNoHit = 0xFFFFFFFFu;  // no child reference: slots stay below kSlotMask
-
 struct Wavefront {
   DBuf<float4> ow[2];           // per path slot: (o.xyz, w)
   DBuf<float4> dk[2];           // (d.xyz, bits of k)
@@ -195,7 +175,6 @@ struct rtg_context {
   int32_t deposit_mode = RTG_DEPOSIT_NEIGHBORS;
   float window_factor = 5.0f;  // point_cloud_context.hpp:163
   rtg::Wavefront wf;
-  rtg::RayOrder ro;
   std::string err;
 };
 

@@ -28,7 +28,7 @@ namespace rtg {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr uint32_t kNoLeaf = kNoHit;
+constexpr uint32_t kNoLeaf = 0xFFFFFFFFu;  // no child reference: slots stay below kSlotMask
 
 __device__ __forceinline__ float safe_inv(float d) {
   if (fabsf(d) < 1e-30f) d = d < 0.0f ? -1e-30f : 1e-30f;
@@ -342,16 +342,6 @@ __device__ float window_deposit(const TraceParams& p, f3 o, f3 d, float t0, floa
   return n > 0 ? (float)((double)w - sum / (double)n) : w;
 }
 
-// source.hpp:20-58 with rectangle_origin_z / (power_)cosine_direction_z:
-// source ray `id` from the top of the box.
-__device__ __forceinline__ void source_ray(const TraceParams& p, uint64_t id, f3& o, f3& d) {
-  const uint4 u = draw4(p.seed, id, 0xFFFFFFFFu, p.job);
-  const float r1 = u01_co(u.x), r2 = u01_co(u.y);
-  o = mk3(p.src_lo[0] + (p.src_hi[0] - p.src_lo[0]) * r1, p.src_lo[1] + (p.src_hi[1] - p.src_lo[1]) * r2,
-          p.box_hi[2]);
-  d = source_dir(p.source_exponent, p.source_ee, u.z, u.w);
-}
-
 // Side-face exit of the x/y box: 0 = x face, 1 = y face, -1 = the ray leaves
 // through the top or bottom first (a miss).
 __device__ __forceinline__ int boundary_exit(const TraceParams& p, f3 o, f3 d, float& tb) {
@@ -417,8 +407,6 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
   constexpr bool kAdj = M == kModeAdjGlobal || M == kModeAdjField;
-  constexpr bool kOrdered = M == kModeForward && !Batched;  // may start from precomputed first hits
-  uint32_t pend = kNoHit;  // local ray index whose precomputed first hit is still to be used
   static_assert(!SHSTACK || STACK * TPB * 4 <= 32768, "a shared stack of at most 32 KB per block");
   constexpr int kSst = SHSTACK ? TPB : 0;
   uint32_t* sstk = nullptr;
@@ -503,17 +491,15 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
               }
               pp = jobs + lo;
               id = pp->ray_begin + (j - __ldg(&prefix[lo]));
-            } else if (kOrdered && p0.order) {
-              pend = __ldg(&p0.order[j]);
-              if (pend >= nrays) {  // not a permutation: count it, trace ray j unordered
-                c_err += 1;
-                pend = (uint32_t)j;
-              }
-              id = p0.ray_begin + pend;
             } else {
               id = p0.ray_begin + j;
             }
-            source_ray(*pp, id, o, d);
+            // source.hpp:20-58 with rectangle_origin_z / (power_)cosine_direction_z
+            const uint4 u = draw4(pp->seed, id, 0xFFFFFFFFu, pp->job);
+            const float r1 = u01_co(u.x), r2 = u01_co(u.y);
+            o = mk3(pp->src_lo[0] + (pp->src_hi[0] - pp->src_lo[0]) * r1,
+                    pp->src_lo[1] + (pp->src_hi[1] - pp->src_lo[1]) * r2, pp->box_hi[2]);
+            d = source_dir(pp->source_exponent, pp->source_ee, u.z, u.w);
             w = 1.0f;
             k = 0;
             nseg = 0;
@@ -553,16 +539,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
     float th, tb = 0.0f;
     int hid;
     uint32_t href;
-    bool hit;
-    if (kOrdered && pend != kNoHit) {  // the first segment's closest hit, found by the ordering pass
-      th = __ldg(&p0.first_t[pend]);
-      hid = __ldg(&p0.first_id[pend]);
-      href = __ldg(&p0.first_ref[pend]);
-      hit = href != kNoHit;
-      pend = kNoHit;
-    } else {
-      hit = closest_hit<STACK, POSTPONE, kSst>(pp->s, o, d, pp->tnear, th, hid, href, c_err, sstk);
-    }
+    const bool hit = closest_hit<STACK, POSTPONE, kSst>(pp->s, o, d, pp->tnear, th, hid, href, c_err, sstk);
     const int axis = boundary_exit(*pp, o, d, tb);
     if (hit && (axis < 0 || th <= tb)) {
       float4 nn;

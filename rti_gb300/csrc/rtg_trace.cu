@@ -26,72 +26,6 @@ __global__ void closest_hit_kernel(const SceneView s, const float* __restrict__ 
   if (e) atomicAdd(errors, e);
 }
 
-// The ordering pass of RTG_ORDER_DEEP_FIRST: the first closest hit of every
-// source ray (the same traversal the path kernel would run for its first
-// segment) and a depth bucket of it, 0 = lowest hit point, kOrderBuckets - 1 =
-// no hit; counts[b] += rays in bucket b.
-template <int STACK>
-__global__ void __launch_bounds__(128) first_hit_kernel(const __grid_constant__ TraceParams p, uint64_t n,
-                                                         float* __restrict__ ft, int32_t* __restrict__ fid,
-                                                         uint32_t* __restrict__ fref, uint8_t* __restrict__ bucket,
-                                                         unsigned int* __restrict__ counts) {
-  __shared__ unsigned int h[kOrderBuckets];
-  if (threadIdx.x < kOrderBuckets) h[threadIdx.x] = 0;
-  __syncthreads();
-  unsigned long long errs = 0;
-  const float zlo = p.box_lo[2];
-  const float scale = (kOrderBuckets - 1) / fmaxf(p.box_hi[2] - p.box_lo[2], 1e-30f);
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
-    f3 o, d;
-    source_ray(p, p.ray_begin + j, o, d);
-    float th;
-    int hid;
-    uint32_t href;
-    const bool hit = closest_hit<STACK, false>(p.s, o, d, p.tnear, th, hid, href, errs);
-    ft[j] = th;
-    fid[j] = hid;
-    fref[j] = hit ? href : kNoHit;
-    int b = kOrderBuckets - 1;
-    if (hit) {
-      const float z = (o.z + d.z * th - zlo) * scale;  // NaN-free: th is finite on a hit
-      b = z < 0.0f ? 0 : (z >= (float)(kOrderBuckets - 2) ? kOrderBuckets - 2 : (int)z);
-    }
-    bucket[j] = (uint8_t)b;
-    atomicAdd(&h[b], 1u);
-  }
-  __syncthreads();
-  if (threadIdx.x < kOrderBuckets && h[threadIdx.x]) atomicAdd(&counts[threadIdx.x], h[threadIdx.x]);
-  if (errs) atomicAdd(&p.tally->errors, errs);
-}
-
-// cursors[b] = rays in buckets below b (one thread).
-__global__ void bucket_offsets_kernel(const unsigned int* __restrict__ counts, unsigned int* __restrict__ cursors) {
-  unsigned int s = 0;
-  for (int b = 0; b < kOrderBuckets; ++b) {
-    cursors[b] = s;
-    s += counts[b];
-  }
-}
-
-// order[cursor[b]++] = j for every ray j, bucket by bucket (warp-aggregated;
-// the order within a bucket is not defined and does not change a result).
-__global__ void __launch_bounds__(256) order_scatter_kernel(uint64_t n, const uint8_t* __restrict__ bucket,
-                                                             unsigned int* __restrict__ cursors,
-                                                             uint32_t* __restrict__ order) {
-  const int lane = threadIdx.x & 31;
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t j = base + threadIdx.x;
-    const bool valid = j < n;
-    const unsigned int b = valid ? bucket[j] : kOrderBuckets;
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
-    const int leader = __ffs(peers) - 1;
-    unsigned int pos = 0;
-    if (valid && lane == leader) pos = atomicAdd(&cursors[b], (unsigned int)__popc(peers));
-    pos = __shfl_sync(0xFFFFFFFFu, pos, leader);
-    if (valid) order[pos + __popc(peers & ((1u << lane) - 1u))] = (uint32_t)j;
-  }
-}
-
 template <int TPB, bool POSTPONE>
 PathKernel forward_kernel(int stack, bool shared) {
   if (stack <= 32) return kernel_for<kModeForward, false, TPB, 32, POSTPONE>(shared);
@@ -161,8 +95,6 @@ int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc) {
     return bad("leaf_tests must be RTG_LEAF_IMMEDIATE or RTG_LEAF_POSTPONED");
   if (lc.stack_memory != RTG_STACK_AUTO && lc.stack_memory != RTG_STACK_LOCAL && lc.stack_memory != RTG_STACK_SHARED)
     return bad("stack_memory must be RTG_STACK_AUTO, RTG_STACK_LOCAL or RTG_STACK_SHARED");
-  if (lc.ray_order != RTG_ORDER_AUTO && lc.ray_order != RTG_ORDER_ID && lc.ray_order != RTG_ORDER_DEEP_FIRST)
-    return bad("ray_order must be RTG_ORDER_AUTO, RTG_ORDER_ID or RTG_ORDER_DEEP_FIRST");
   return RTG_OK;
 }
 
@@ -181,47 +113,11 @@ SceneView scene_view(rtg_context* ctx) {
   return s;
 }
 
-namespace {
-
-// The deep-first order of RTG_ORDER_DEEP_FIRST: the first-hit pass, the bucket
-// offsets and the scatter, all on st; fills p.order and p.first_*.
-int order_deep_first(rtg_context* ctx, TraceParams& p, uint64_t nrays, int stack, int sms, cudaStream_t st) {
-  RayOrder& ro = ctx->ro;
-  RTG_TRY(dalloc(ctx, ro.order, (size_t)nrays, "ray order"));
-  RTG_TRY(dalloc(ctx, ro.t, (size_t)nrays, "first hits"));
-  RTG_TRY(dalloc(ctx, ro.id, (size_t)nrays, "first hits"));
-  RTG_TRY(dalloc(ctx, ro.ref, (size_t)nrays, "first hits"));
-  RTG_TRY(dalloc(ctx, ro.bucket, (size_t)nrays, "ray buckets"));
-  RTG_TRY(dalloc(ctx, ro.counts, (size_t)(2 * kOrderBuckets), "bucket counts"));
-  RTG_CUDA(ctx, cudaMemsetAsync(ro.counts.p, 0, kOrderBuckets * sizeof(unsigned int), st));
-  const unsigned grid = (unsigned)(sms * 8);
-  if (stack <= 32)
-    first_hit_kernel<32><<<grid, 128, 0, st>>>(p, nrays, ro.t.p, ro.id.p, ro.ref.p, ro.bucket.p, ro.counts.p);
-  else if (stack <= 64)
-    first_hit_kernel<64><<<grid, 128, 0, st>>>(p, nrays, ro.t.p, ro.id.p, ro.ref.p, ro.bucket.p, ro.counts.p);
-  else
-    first_hit_kernel<256><<<grid, 128, 0, st>>>(p, nrays, ro.t.p, ro.id.p, ro.ref.p, ro.bucket.p, ro.counts.p);
-  RTG_CUDA(ctx, cudaGetLastError());
-  bucket_offsets_kernel<<<1, 1, 0, st>>>(ro.counts.p, ro.counts.p + kOrderBuckets);
-  RTG_CUDA(ctx, cudaGetLastError());
-  order_scatter_kernel<<<(unsigned)(sms * 8), 256, 0, st>>>(nrays, ro.bucket.p, ro.counts.p + kOrderBuckets,
-                                                            ro.order.p);
-  RTG_CUDA(ctx, cudaGetLastError());
-  p.order = ro.order.p;
-  p.first_t = ro.t.p;
-  p.first_id = ro.id.p;
-  p.first_ref = ro.ref.p;
-  return RTG_OK;
-}
-
-}  // namespace
-
 int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int mode) {
   const rtg_launch_config& lc = ctx->lc;
   const int stack = stack_for(lc.stack_depth, ctx->g.depth);
   TraceParams p = p_in;
   p.packet = lc.packet;
-  p.order = nullptr;
   const uint64_t nrays = p.ray_end - p.ray_begin;
   // the window deposit has a kernel of its own (megakernel or plain schedule)
   if (mode == kModeForward && p.window) mode = kModeWindow;
@@ -247,10 +143,6 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
   const uint64_t need = (nrays + tpb - 1) / tpb;
   if (need < blocks || p.plain) blocks = need > 0 ? need : 1;
   if (blocks > 0x7FFFFFFFull) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "too many rays for a plain launch");
-  const bool deep_first = mode == kModeForward && !p.plain && nrays <= (1ull << 27) &&
-                          (lc.ray_order == RTG_ORDER_DEEP_FIRST ||
-                           (lc.ray_order == RTG_ORDER_AUTO && nrays >= (1ull << 20)));
-  if (deep_first) RTG_TRY(order_deep_first(ctx, p, nrays, stack, sms, st));
   kern<<<(unsigned)blocks, tpb, 0, st>>>(p, nullptr, nullptr, 0);
   RTG_CUDA(ctx, cudaGetLastError());
   return RTG_OK;

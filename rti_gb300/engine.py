@@ -165,9 +165,8 @@ class Engine:
 
     def set_launch_config(self, threads_per_block: int = 128, packet: int = 1, stack_depth: int = 0,
                           scheduling: int = L.RTG_SCHED_MEGAKERNEL, leaf_tests: int = L.RTG_LEAF_IMMEDIATE,
-                          stack_memory: int = L.RTG_STACK_AUTO, ray_order: int = L.RTG_ORDER_AUTO):
-        lc = L.RtgLaunchConfig(threads_per_block, packet, stack_depth, scheduling, leaf_tests, stack_memory,
-                               ray_order)
+                          stack_memory: int = L.RTG_STACK_AUTO):
+        lc = L.RtgLaunchConfig(threads_per_block, packet, stack_depth, scheduling, leaf_tests, stack_memory)
         self._check(self._L.rtg_set_launch_config(self._h, C.byref(lc)))
 
     @property

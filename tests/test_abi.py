@@ -55,7 +55,7 @@ def test_launch_config_default(rtg_lib):
     rtg_lib.rtg_launch_config_default(C.byref(lc))
     assert lc.as_dict() == {"threads_per_block": 128, "packet": 1, "stack_depth": 0,
                             "scheduling": _lib.RTG_SCHED_MEGAKERNEL, "leaf_tests": _lib.RTG_LEAF_IMMEDIATE,
-                            "stack_memory": _lib.RTG_STACK_AUTO, "ray_order": _lib.RTG_ORDER_AUTO}
+                            "stack_memory": _lib.RTG_STACK_AUTO}
 
 
 LAYOUT_C = r"""
@@ -74,7 +74,7 @@ int main(void) {
   F(rtg_device_view, estimates); F(rtg_device_view, n);
   printf("rtg_launch_config %zu\n", sizeof(rtg_launch_config));
   F(rtg_launch_config, packet); F(rtg_launch_config, stack_depth); F(rtg_launch_config, scheduling);
-  F(rtg_launch_config, leaf_tests); F(rtg_launch_config, stack_memory); F(rtg_launch_config, ray_order);
+  F(rtg_launch_config, leaf_tests); F(rtg_launch_config, stack_memory);
   return 0;
 }
 """

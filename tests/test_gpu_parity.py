@@ -138,14 +138,11 @@ def test_neighbors_random_cloud(eng, oracle_lib):
     assert np.array_equal(rg, rc) and np.array_equal(cg, cc)
 
 
-@pytest.mark.parametrize("order", [1, 2], ids=["id-order", "deep-first"])
 @pytest.mark.parametrize("bound", [1, 0], ids=["periodic", "reflective"])
-def test_trace_trench_matches_oracle(eng, trench, oracle_lib, bound, order):
+def test_trace_trench_matches_oracle(eng, trench, oracle_lib, bound):
     _upload_discs(eng, trench, sticking=0.1, x_bound=bound, y_bound=bound)
     n = 200000
-    eng.set_launch_config(ray_order=order)
     g = _gpu_trace(eng, n, seed=11)
-    eng.set_launch_config()
     s = oracle_lib.Scene(trench.xyzr, trench.normals)
     s.neighbors()
     cfg = oracle_lib.make_config(trench.box_lo, trench.box_hi, sticking=0.1, x_bound=bound, y_bound=bound, seed=11)
@@ -154,15 +151,12 @@ def test_trace_trench_matches_oracle(eng, trench, oracle_lib, bound, order):
     _compare_trace(g, c, trench.n)
 
 
-@pytest.mark.parametrize("order", [1, 2], ids=["id-order", "deep-first"])
-def test_trace_hole_mixed_reflection_matches_oracle(eng, hole, oracle_lib, order):
+def test_trace_hole_mixed_reflection_matches_oracle(eng, hole, oracle_lib):
     eng.upload_triangles(hole.vertices, hole.indices)
     eng.configure(box=(hole.box_lo, hole.box_hi), sticking=0.01, reflection=2, specular_fraction=0.1,
                   x_bound=1, y_bound=1, reset=True)
     n = 100000
-    eng.set_launch_config(ray_order=order)
     g = _gpu_trace(eng, n, seed=3)
-    eng.set_launch_config()
     s = oracle_lib.Scene(tri_vertices=hole.vertices, tri_indices=hole.indices)
     cfg = oracle_lib.make_config(hole.box_lo, hole.box_hi, sticking=0.01, reflection=2, specular_fraction=0.1,
                                  seed=3)
