@@ -340,6 +340,8 @@ def run_ours(args):
     eng.upload_triangles(h.vertices, h.indices)
     eng.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
                   x_bound=1, y_bound=1, source_exponent=1.0)
+    if args.sweep:
+        return ray_sweep(eng, [int(float(x)) for x in args.sweep.split(",")])
     # one dedicated stream for the flush, the events and librtg's kernels
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
@@ -528,6 +530,26 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def ray_sweep(eng, sizes):
+    """Path-kernel time (best of 3) against the number of rays on the bench
+    workload, and the least-squares line T = tail + slope * rays: the intercept
+    is the time the longest paths add after the throughput phase."""
+    eng.trace(1_000_000, seed=0)
+    rows = []
+    for n in sizes:
+        ks = []
+        for k in range(3):
+            eng.trace(n, seed=k + 1)
+            ks.append(eng.tally().kernel_ms)
+        rows.append((n, min(ks)))
+    x = np.array([r[0] for r in rows], dtype=np.float64)
+    y = np.array([r[1] for r in rows])
+    slope, tail = np.polyfit(x, y, 1) if len(rows) > 1 else (float("nan"), float("nan"))
+    print(json.dumps({"sweep": [{"rays": n, "kernel_ms": round(ms, 3)} for n, ms in rows],
+                      "tail_ms": round(float(tail), 2), "ms_per_1e6_rays": round(float(slope) * 1e6, 4),
+                      "rays_per_s_without_tail": 1e3 / float(slope) if slope > 0 else None}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -545,6 +567,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-rays", type=int, default=2_000_000, help="rays per job of the batch block")
     ap.add_argument("--no-rough", action="store_true")
+    ap.add_argument("--sweep", default="", help="comma-separated ray counts: path-kernel time against rays "
+                                                "(the tail analysis), printed instead of the bench line")
     ap.add_argument("--rough-rays", type=int, default=100_000_000, help="rays of the rough-surface block")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
