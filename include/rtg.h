@@ -132,10 +132,11 @@ typedef struct rtg_launch_config {
 /* stack_memory: per-thread local memory (cached in L1 beside the tree), or
  * shared memory (one column per thread, conflict-free), which leaves L1 to
  * the tree but takes its share of the SM's L1/shared capacity.  Shared is
- * used where the stack fits 32 KB per block (stack entries x block size x 4 B)
- * and falls back to local otherwise.  AUTO: shared when the tree and the
- * primitive records outgrow the L2 cache (measured: a 4.19 M-disc surface
- * traces 5 % faster with it, a 200 k-triangle surface 2 % slower). */
+ * used where the stack fits 16 KB per block (stack entries x block size x 4 B)
+ * and falls back to local otherwise (larger shared stacks starve L1).  AUTO:
+ * shared when the tree and the primitive records outgrow the L2 cache
+ * (measured: a 4.19 M-disc surface traces 6 % faster with it, a 200 k-triangle
+ * surface 2 % slower). */
 #define RTG_STACK_AUTO 0
 #define RTG_STACK_LOCAL 1
 #define RTG_STACK_SHARED 2

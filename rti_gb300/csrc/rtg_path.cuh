@@ -401,13 +401,13 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // the abort flag are the batch's (p0).  TPB threads per block and 1024 / TPB
 // resident blocks per SM as the register target (64 registers per thread).
 // SHSTACK = true: the traversal stacks of the block live in shared memory
-// (STACK x TPB entries, at most 32 KB).
+// (STACK x TPB entries, at most 16 KB).
 template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false, bool SHSTACK = false>
 __global__ void __launch_bounds__(TPB, 1024 / TPB)
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
   constexpr bool kAdj = M == kModeAdjGlobal || M == kModeAdjField;
-  static_assert(!SHSTACK || STACK * TPB * 4 <= 32768, "a shared stack of at most 32 KB per block");
+  static_assert(!SHSTACK || STACK * TPB * 4 <= 16384, "a shared stack of at most 16 KB per block");
   constexpr int kSst = SHSTACK ? TPB : 0;
   uint32_t* sstk = nullptr;
   if constexpr (SHSTACK) {
@@ -690,10 +690,11 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
 using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_t*, int);
 
 // The instantiation of trace_paths_kernel with its stack in shared memory
-// when `shared` asks for it and it fits 32 KB per block, else in local memory.
+// when `shared` asks for it and it fits 16 KB per block (8 blocks then leave
+// half of the SM's L1/shared capacity to L1), else in local memory.
 template <int M, bool Batched, int TPB, int STACK, bool POSTPONE>
 PathKernel kernel_for(bool shared) {
-  if constexpr (STACK * TPB * 4 <= 32768) {
+  if constexpr (STACK * TPB * 4 <= 16384) {
     if (shared) return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, true>;
   }
   return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, false>;

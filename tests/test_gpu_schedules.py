@@ -18,7 +18,7 @@ CONFIGS = [(64, 1, 0, MK), (256, 8, 0, MK), (128, 32, 256, MK), (128, 1, 32, MK)
            (256, 1, 256, WF), (64, 1, 64, WF), (128, 1, 0, PL), (256, 1, 64, PL),
            (128, 1, 0, MK, 1), (256, 8, 256, MK, 1), (128, 1, 0, PL, 1),
            (128, 1, 0, MK, 0, SHARED), (64, 8, 64, MK, 1, SHARED), (256, 1, 0, PL, 0, SHARED),
-           (128, 1, 64, MK, 0, SHARED), (128, 1, 0, MK, 0, LOCAL), (256, 1, 256, MK, 0, SHARED)]
+           (128, 1, 64, MK, 0, SHARED), (128, 1, 0, MK, 0, LOCAL), (256, 1, 256, MK, 0, SHARED), (64, 1, 64, MK, 0, SHARED)]
 
 
 @pytest.fixture(scope="module")
