@@ -101,9 +101,9 @@ __device__ __forceinline__ void test_leaf(const SceneView& s, uint32_t ref, cons
 // SST = 0: the stack is a per-thread local array; SST > 0: it is a column of
 // shared memory, entry i at sstk[i * SST] (SST = the block size, so the lanes
 // of a warp always hit distinct banks).
-template <int STACK, bool POSTPONE, int SST = 0>
+template <int STACK, bool POSTPONE, int SST = 0, typename Count = unsigned long long>
 __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& bt, int& bid, uint32_t& bref,
-                            unsigned long long& errs, uint32_t* sstk = nullptr) {
+                            Count& errs, uint32_t* sstk = nullptr) {
   Ray r;
   r.o = o;
   r.d = d;
@@ -241,7 +241,7 @@ __device__ __forceinline__ bool overlaps(float lx, float hx, float ly, float hy,
 // Calls visit(ref) once for every leaf whose box the ray overlaps within
 // [tlo, thi].  errs counts stack overflows and iteration-limit trips.
 template <int STACK, typename Visit>
-__device__ void leaves_in_interval(const SceneView& s, const Ray& r, float tlo, float thi, unsigned long long& errs,
+__device__ void leaves_in_interval(const SceneView& s, const Ray& r, float tlo, float thi, uint32_t& errs,
                                    Visit visit) {
   uint32_t stack[STACK];
   int sp = 0;
@@ -292,7 +292,7 @@ __device__ void leaves_in_interval(const SceneView& s, const Ray& r, float tlo, 
 // within a factor 2^28 of each other (always for a global sticking).
 template <int STACK>
 __device__ float window_deposit(const TraceParams& p, f3 o, f3 d, float t0, float tbox, uint32_t ref, float w,
-                                unsigned long long& c_tot, unsigned long long& c_nb, unsigned long long& errs) {
+                                uint32_t& c_tot, uint32_t& c_nb, uint32_t& errs) {
   Ray r;
   r.o = o;
   r.d = d;
@@ -337,8 +337,8 @@ __device__ float window_deposit(const TraceParams& p, f3 o, f3 d, float t0, floa
       n += 1;
     }
   });
-  c_tot += n;
-  c_nb += n > 0 ? n - 1 : 0;
+  c_tot += (uint32_t)n;
+  c_nb += n > 0 ? (uint32_t)(n - 1) : 0u;
   return n > 0 ? (float)((double)w - sum / (double)n) : w;
 }
 
@@ -417,7 +417,9 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
   const TraceParams* pp = &p0;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
-  unsigned long long c_hit = 0, c_non = 0, c_tot = 0, c_seg = 0, c_trunc = 0, c_nb = 0, c_err = 0;
+  // per-lane counters, summed over the warp at the end (32 bits: a lane traces
+  // far fewer than 2^32 segments)
+  uint32_t c_hit = 0, c_non = 0, c_tot = 0, c_seg = 0, c_trunc = 0, c_nb = 0, c_err = 0;
   bool active = false, exhausted = false;
   uint64_t id = 0;
   f3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
@@ -669,21 +671,17 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB)
       atomicAdd(&pp->adj_scalars[1], acc_n);
     }
   }
-  c_hit = warp_sum(c_hit);
-  c_non = warp_sum(c_non);
-  c_tot = warp_sum(c_tot);
-  c_seg = warp_sum(c_seg);
-  c_trunc = warp_sum(c_trunc);
-  c_nb = warp_sum(c_nb);
-  c_err = warp_sum(c_err);
+  const unsigned long long s_hit = warp_sum(c_hit), s_non = warp_sum(c_non), s_tot = warp_sum(c_tot);
+  const unsigned long long s_seg = warp_sum(c_seg), s_trunc = warp_sum(c_trunc), s_nb = warp_sum(c_nb);
+  const unsigned long long s_err = warp_sum(c_err);
   if (lane == 0) {
-    atomicAdd(&p0.tally->hitc, c_hit);
-    atomicAdd(&p0.tally->nonhitc, c_non);
-    atomicAdd(&p0.tally->total, c_tot);
-    atomicAdd(&p0.tally->segments, c_seg);
-    atomicAdd(&p0.tally->truncated, c_trunc);
-    atomicAdd(&p0.tally->nb_deposits, c_nb);
-    atomicAdd(&p0.tally->errors, c_err);
+    atomicAdd(&p0.tally->hitc, s_hit);
+    atomicAdd(&p0.tally->nonhitc, s_non);
+    atomicAdd(&p0.tally->total, s_tot);
+    atomicAdd(&p0.tally->segments, s_seg);
+    atomicAdd(&p0.tally->truncated, s_trunc);
+    atomicAdd(&p0.tally->nb_deposits, s_nb);
+    atomicAdd(&p0.tally->errors, s_err);
   }
 }
 
