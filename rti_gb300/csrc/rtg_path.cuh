@@ -399,11 +399,13 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // of `njobs` jobs (prefix[j] = first global id of job j) and trace each with
 // its job's parameters (scene, configuration, accumulators); the counters and
 // the abort flag are the batch's (p0).  TPB threads per block and 1024 / TPB
-// resident blocks per SM as the register target (64 registers per thread).
+// resident blocks per SM as the register target (64 registers per thread);
+// forward traces with 128 threads target 9 blocks (56 registers, a few spilled:
+// the extra warps hide more latency than the spills cost).
 // SHSTACK = true: the traversal stacks of the block live in shared memory
 // (STACK x TPB entries, at most 16 KB).
 template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false, bool SHSTACK = false>
-__global__ void __launch_bounds__(TPB, 1024 / TPB)
+__global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 : 1024) / TPB)
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
   constexpr bool kAdj = M == kModeAdjGlobal || M == kModeAdjField;
