@@ -90,90 +90,258 @@ namespace {
 
 void resolve_box(rtg_context* ctx) { box_for(ctx->cfg, ctx->g, ctx->box_lo, ctx->box_hi); }
 
+// ---- upload: the host arrays are copied as they are and checked and
+// converted on the device; one small read-back carries the verdict ----
+
+// Bounds and first offending index of an upload.
+struct UploadCheck {
+  float lo[3], hi[3];           // disc centres, or the vertices the triangles use
+  float rmax;                   // largest disc radius
+  unsigned long long bad;       // lowest disc / vertex index that fails its check, or ~0
+  unsigned long long bad_tri;   // lowest triangle with an index out of range, or ~0
+};
+
+__device__ __forceinline__ void atomic_min_f(float* a, float v) {  // order of IEEE bits as integers
+  if (__float_as_int(v) >= 0) atomicMin((int*)a, __float_as_int(v));
+  else atomicMax((unsigned int*)a, __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float* a, float v) {
+  if (__float_as_int(v) >= 0) atomicMax((int*)a, __float_as_int(v));
+  else atomicMin((unsigned int*)a, __float_as_uint(v));
+}
+
+// Warp minima/maxima of (x, y, z), then one atomic per warp.
+__device__ __forceinline__ void bounds_add(UploadCheck* c, float x, float y, float z, bool valid) {
+  float l[3] = {valid ? x : FLT_MAX, valid ? y : FLT_MAX, valid ? z : FLT_MAX};
+  float h[3] = {valid ? x : -FLT_MAX, valid ? y : -FLT_MAX, valid ? z : -FLT_MAX};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      l[a] = fminf(l[a], __shfl_xor_sync(0xFFFFFFFFu, l[a], o));
+      h[a] = fmaxf(h[a], __shfl_xor_sync(0xFFFFFFFFu, h[a], o));
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int a = 0; a < 3; ++a) {
+      atomic_min_f(&c->lo[a], l[a]);
+      atomic_max_f(&c->hi[a], h[a]);
+    }
+}
+
+__global__ void check_init_kernel(UploadCheck* c) {
+  for (int a = 0; a < 3; ++a) {
+    c->lo[a] = FLT_MAX;
+    c->hi[a] = -FLT_MAX;
+  }
+  c->rmax = 0.0f;
+  c->bad = ~0ull;
+  c->bad_tri = ~0ull;
+}
+
+__device__ __forceinline__ bool finite3_d(float x, float y, float z) {
+  return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+// Disc i: finite centre, normal and radius, radius > 0, unit normal (within
+// 1e-3); writes (centre, r) and (normal, 0).  Grid-stride; whole warps.
+__global__ void disc_check_kernel(const float* __restrict__ pts, const float* __restrict__ nrm,
+                                  const float* __restrict__ rad, int64_t n, float4* __restrict__ cr,
+                                  float4* __restrict__ nn, UploadCheck* c) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int64_t i = base + threadIdx.x;
+    const bool in = i < n;
+    float p[3] = {0, 0, 0}, q[3] = {0, 0, 1}, r = 1.0f;
+    if (in)
+      for (int a = 0; a < 3; ++a) {
+        p[a] = pts[3 * i + a];
+        q[a] = nrm[3 * i + a];
+      }
+    if (in) r = rad[i];
+    bool ok = finite3_d(p[0], p[1], p[2]) && finite3_d(q[0], q[1], q[2]) && isfinite(r) && r > 0.0f;
+    if (ok) {
+      const float l2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+      ok = fabsf(sqrtf(l2) - 1.0f) <= 1e-3f;
+    }
+    if (in && !ok) atomicMin(&c->bad, (unsigned long long)i);
+    if (in) {
+      cr[i] = make_float4(p[0], p[1], p[2], r);
+      nn[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    const bool v = in && ok;
+    bounds_add(c, p[0], p[1], p[2], v);
+    float rm = v ? r : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rm = fmaxf(rm, __shfl_xor_sync(0xFFFFFFFFu, rm, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_f(&c->rmax, rm);
+  }
+}
+
+// Vertex i: finite; writes (x, y, z, 0).
+__global__ void vertex_check_kernel(const float* __restrict__ v, int64_t nv, float4* __restrict__ out,
+                                    UploadCheck* c) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+    const float x = v[3 * i], y = v[3 * i + 1], z = v[3 * i + 2];
+    if (!finite3_d(x, y, z)) atomicMin(&c->bad, (unsigned long long)i);
+    out[i] = make_float4(x, y, z, 0.0f);
+  }
+}
+
+// Triangle t: its three indices below nv; bounds over the vertices it uses.
+__global__ void triangle_check_kernel(const uint32_t* __restrict__ idx, int64_t nt, int64_t nv,
+                                      const float4* __restrict__ vert, UploadCheck* c) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nt; base += stride) {
+    const int64_t t = base + threadIdx.x;
+    const bool in = t < nt;
+    for (int k = 0; k < 3; ++k) {
+      const uint32_t q = in ? idx[3 * t + k] : 0u;
+      const bool ok = in && (int64_t)q < nv;
+      if (in && !ok) atomicMin(&c->bad_tri, (unsigned long long)t);
+      float4 p = make_float4(0, 0, 0, 0);
+      if (ok) p = vert[q];
+      bounds_add(c, p.x, p.y, p.z, ok);
+    }
+  }
+}
+
+unsigned grid_for(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 4096));
+}
+
 int upload_discs_impl(rtg_context* ctx, const float* pts, const float* nrm, const float* rad, int64_t n,
                       bool rebuild) {
   if (n < 0 || (n > 0 && (!pts || !nrm || !rad)))
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "discs: null array or negative count");
-  std::vector<float4> cr((size_t)n), nn((size_t)n);
-  Geometry& g = ctx->g;
-  float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-  float rmax = 0.0f;
-  for (int64_t i = 0; i < n; ++i) {
-    const float* p = pts + 3 * i;
-    const float* q = nrm + 3 * i;
-    const float r = rad[i];
-    if (!finite3(p) || !finite3(q) || !std::isfinite(r) || !(r > 0.0f))
-      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
-                       "disc " + std::to_string(i) + ": non-finite value or radius <= 0");
-    const float l2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-    if (!(std::fabs(std::sqrt(l2) - 1.0f) <= 1e-3f))
-      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "disc " + std::to_string(i) + ": normal is not unit length");
-    cr[(size_t)i] = make_float4(p[0], p[1], p[2], r);
-    nn[(size_t)i] = make_float4(q[0], q[1], q[2], 0.0f);
-    for (int a = 0; a < 3; ++a) {
-      cmin[a] = std::min(cmin[a], p[a]);
-      cmax[a] = std::max(cmax[a], p[a]);
-    }
-    rmax = std::max(rmax, r);
-  }
-  if (!rebuild && n != g.nd)
+  if (!rebuild && n != ctx->g.nd)
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "update_discs: the disc count must not change");
-  g.nd = n;
+  Geometry& g = ctx->g;
+  cudaStream_t st = ctx->stream;
+  UploadCheck h{};
   for (int a = 0; a < 3; ++a) {
-    g.cmin[a] = cmin[a];
-    g.cmax[a] = cmax[a];
+    h.lo[a] = FLT_MAX;
+    h.hi[a] = -FLT_MAX;
   }
-  g.rmax = rmax;
-  RTG_TRY(dalloc(ctx, g.disc_cr_by_id, (size_t)(n > 0 ? n : 1), "discs"));
-  RTG_TRY(dalloc(ctx, g.disc_n_by_id, (size_t)(n > 0 ? n : 1), "disc normals"));
+  h.bad = ~0ull;
+  DBuf<float> raw;
+  DBuf<float4> cr, nn;
+  DBuf<UploadCheck> chk;
+  int rc = RTG_OK;
   if (n > 0) {
-    RTG_CUDA(ctx, cudaMemcpyAsync(g.disc_cr_by_id.p, cr.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
-                                  ctx->stream));
-    RTG_CUDA(ctx, cudaMemcpyAsync(g.disc_n_by_id.p, nn.data(), n * sizeof(float4), cudaMemcpyHostToDevice,
-                                  ctx->stream));
+    rc = talloc(ctx, raw, (size_t)(7 * n), st, "disc upload");
+    if (rc == RTG_OK) rc = talloc(ctx, cr, (size_t)n, st, "disc upload");
+    if (rc == RTG_OK) rc = talloc(ctx, nn, (size_t)n, st, "disc upload");
+    if (rc == RTG_OK) rc = talloc(ctx, chk, 1, st, "disc upload");
+    cudaError_t e = cudaSuccess;
+    if (rc == RTG_OK) e = cudaMemcpyAsync(raw.p, pts, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (rc == RTG_OK && e == cudaSuccess)
+      e = cudaMemcpyAsync(raw.p + 3 * n, nrm, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (rc == RTG_OK && e == cudaSuccess)
+      e = cudaMemcpyAsync(raw.p + 6 * n, rad, n * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (rc == RTG_OK && e == cudaSuccess) {
+      check_init_kernel<<<1, 1, 0, st>>>(chk.p);
+      disc_check_kernel<<<grid_for(n), 256, 0, st>>>(raw.p, raw.p + 3 * n, raw.p + 6 * n, n, cr.p, nn.p, chk.p);
+      e = cudaGetLastError();
+    }
+    if (rc == RTG_OK && e == cudaSuccess) e = cudaMemcpyAsync(&h, chk.p, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (rc == RTG_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "disc upload");
+    if (rc == RTG_OK && h.bad != ~0ull) {  // the message of the first offending disc, as the host sees it
+      const int64_t i = (int64_t)h.bad;
+      const float* q = nrm + 3 * i;
+      const bool finite = finite3(pts + 3 * i) && finite3(q) && std::isfinite(rad[i]) && rad[i] > 0.0f;
+      rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
+                     "disc " + std::to_string(i) +
+                         (finite ? ": normal is not unit length" : ": non-finite value or radius <= 0"));
+    }
   }
-  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return RTG_OK;
+  if (rc == RTG_OK) {
+    g.nd = n;
+    for (int a = 0; a < 3; ++a) {
+      g.cmin[a] = h.lo[a];
+      g.cmax[a] = h.hi[a];
+    }
+    g.rmax = h.rmax;
+    rc = dalloc(ctx, g.disc_cr_by_id, (size_t)(n > 0 ? n : 1), "discs");
+    if (rc == RTG_OK) rc = dalloc(ctx, g.disc_n_by_id, (size_t)(n > 0 ? n : 1), "disc normals");
+    cudaError_t e = cudaSuccess;
+    if (rc == RTG_OK && n > 0)
+      e = cudaMemcpyAsync(g.disc_cr_by_id.p, cr.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+    if (rc == RTG_OK && n > 0 && e == cudaSuccess)
+      e = cudaMemcpyAsync(g.disc_n_by_id.p, nn.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "disc upload");
+  }
+  tfree(raw, st);
+  tfree(cr, st);
+  tfree(nn, st);
+  tfree(chk, st);
+  return rc;
 }
 
 int upload_triangles_impl(rtg_context* ctx, const float* vertices, const uint32_t* indices, int64_t nv,
                           int64_t nt) {
-  if (nv < 0 || nt < 0 || (nt > 0 && (!vertices || !indices)))
+  if (nv < 0 || nt < 0 || (nt > 0 && (!vertices || !indices)) || (nv > 0 && !vertices))
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "triangles: null array or negative count");
   Geometry& g = ctx->g;
-  std::vector<float4> v((size_t)nv);
-  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-  for (int64_t i = 0; i < nv; ++i) {
-    if (!finite3(vertices + 3 * i))
-      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "vertex " + std::to_string(i) + " is not finite");
-    v[(size_t)i] = make_float4(vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2], 0.0f);
-  }
-  for (int64_t t = 0; t < nt; ++t)
-    for (int k = 0; k < 3; ++k) {
-      const uint32_t idx = indices[3 * t + k];
-      if ((int64_t)idx >= nv)
-        return set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
-                         "triangle " + std::to_string(t) + ": vertex index out of range");
-      for (int a = 0; a < 3; ++a) {
-        lo[a] = std::min(lo[a], vertices[3 * (int64_t)idx + a]);
-        hi[a] = std::max(hi[a], vertices[3 * (int64_t)idx + a]);
-      }
-    }
-  g.nt = nt;
-  g.nv = nv;
+  cudaStream_t st = ctx->stream;
+  UploadCheck h{};
   for (int a = 0; a < 3; ++a) {
-    g.tri_min[a] = lo[a];
-    g.tri_max[a] = hi[a];
+    h.lo[a] = FLT_MAX;
+    h.hi[a] = -FLT_MAX;
   }
-  RTG_TRY(dalloc(ctx, g.tri_v, (size_t)(nv > 0 ? nv : 1), "vertices"));
-  RTG_TRY(dalloc(ctx, g.tri_idx, (size_t)(3 * (nt > 0 ? nt : 1)), "triangle indices"));
-  if (nv > 0)
-    RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_v.p, v.data(), nv * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
-  if (nt > 0)
-    RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_idx.p, indices, 3 * nt * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                                  ctx->stream));
-  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return RTG_OK;
+  h.bad = ~0ull;
+  h.bad_tri = ~0ull;
+  DBuf<float> raw;
+  DBuf<float4> v4;
+  DBuf<uint32_t> ix;
+  DBuf<UploadCheck> chk;
+  int rc = RTG_OK;
+  if (nv > 0 || nt > 0) {
+    rc = talloc(ctx, chk, 1, st, "triangle upload");
+    if (rc == RTG_OK && nv > 0) rc = talloc(ctx, raw, (size_t)(3 * nv), st, "triangle upload");
+    if (rc == RTG_OK && nv > 0) rc = talloc(ctx, v4, (size_t)nv, st, "triangle upload");
+    if (rc == RTG_OK && nt > 0) rc = talloc(ctx, ix, (size_t)(3 * nt), st, "triangle upload");
+    cudaError_t e = cudaSuccess;
+    if (rc == RTG_OK && nv > 0) e = cudaMemcpyAsync(raw.p, vertices, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (rc == RTG_OK && nt > 0 && e == cudaSuccess)
+      e = cudaMemcpyAsync(ix.p, indices, 3 * nt * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (rc == RTG_OK && e == cudaSuccess) {
+      check_init_kernel<<<1, 1, 0, st>>>(chk.p);
+      if (nv > 0) vertex_check_kernel<<<grid_for(nv), 256, 0, st>>>(raw.p, nv, v4.p, chk.p);
+      if (nt > 0) triangle_check_kernel<<<grid_for(nt), 256, 0, st>>>(ix.p, nt, nv, v4.p, chk.p);
+      e = cudaGetLastError();
+    }
+    if (rc == RTG_OK && e == cudaSuccess) e = cudaMemcpyAsync(&h, chk.p, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (rc == RTG_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "triangle upload");
+    if (rc == RTG_OK && h.bad != ~0ull)
+      rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "vertex " + std::to_string(h.bad) + " is not finite");
+    else if (rc == RTG_OK && h.bad_tri != ~0ull)
+      rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
+                     "triangle " + std::to_string(h.bad_tri) + ": vertex index out of range");
+  }
+  if (rc == RTG_OK) {
+    g.nt = nt;
+    g.nv = nv;
+    for (int a = 0; a < 3; ++a) {
+      g.tri_min[a] = h.lo[a];
+      g.tri_max[a] = h.hi[a];
+    }
+    rc = dalloc(ctx, g.tri_v, (size_t)(nv > 0 ? nv : 1), "vertices");
+    if (rc == RTG_OK) rc = dalloc(ctx, g.tri_idx, (size_t)(3 * (nt > 0 ? nt : 1)), "triangle indices");
+    cudaError_t e = cudaSuccess;
+    if (rc == RTG_OK && nv > 0) e = cudaMemcpyAsync(g.tri_v.p, v4.p, nv * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+    if (rc == RTG_OK && nt > 0 && e == cudaSuccess)
+      e = cudaMemcpyAsync(g.tri_idx.p, ix.p, 3 * nt * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "triangle upload");
+  }
+  tfree(raw, st);
+  tfree(v4, st);
+  tfree(ix, st);
+  tfree(chk, st);
+  return rc;
 }
 
 }  // namespace
