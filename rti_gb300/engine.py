@@ -274,8 +274,17 @@ class Engine:
         s = None if stream is None else C.c_void_p(int(stream) if int(stream) != 0 else 1)
         self._check(self._L.rtg_get_mc_estimates_noalloc(self._h, C.c_void_p(int(d_out)), s))
 
-    def hit_counts(self) -> np.ndarray:
-        out = np.zeros(self.num_primitives, dtype=np.uint64)
+    def _out(self, out, dtype):
+        """A result array: the caller's (e.g. pinned host memory) after a shape/type check, or a new one."""
+        n = self.num_primitives
+        if out is None:
+            return np.zeros(n, dtype=dtype)
+        if out.dtype != dtype or out.shape != (n,) or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a contiguous {np.dtype(dtype).name} array of {n} elements")
+        return out
+
+    def hit_counts(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = self._out(out, np.uint64)
         self._check(self._L.rtg_get_hit_counts(self._h, _ptr(out, L._u64p)))
         return out
 
@@ -285,9 +294,9 @@ class Engine:
         self._check(self._L.rtg_get_accumulators(self._h, *[_ptr(x, L._f64p) for x in s]))
         return s
 
-    def values(self) -> np.ndarray:
+    def values(self, out: np.ndarray | None = None) -> np.ndarray:
         """S1 (the flux per primitive, hit_accumulator::get_values) alone."""
-        out = np.zeros(self.num_primitives)
+        out = self._out(out, np.float64)
         self._check(self._L.rtg_get_accumulators(self._h, _ptr(out, L._f64p), None, None, None))
         return out
 
