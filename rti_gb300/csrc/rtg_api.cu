@@ -211,137 +211,150 @@ unsigned grid_for(int64_t n) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 4096));
 }
 
-int upload_discs_impl(rtg_context* ctx, const float* pts, const float* nrm, const float* rad, int64_t n,
-                      bool rebuild) {
-  if (n < 0 || (n > 0 && (!pts || !nrm || !rad)))
-    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "discs: null array or negative count");
-  if (!rebuild && n != ctx->g.nd)
-    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "update_discs: the disc count must not change");
-  Geometry& g = ctx->g;
-  cudaStream_t st = ctx->stream;
-  UploadCheck h{};
+// An upload checked on the device and not yet part of the context.
+struct Staged {
+  int64_t nd = 0, nv = 0, nt = 0;
+  bool discs = false, triangles = false;
+  UploadCheck hd{}, ht{};
+  DBuf<float4> cr, nn, v4;
+  DBuf<uint32_t> ix;
+};
+
+void release(Staged& sg, cudaStream_t st) {
+  tfree(sg.cr, st);
+  tfree(sg.nn, st);
+  tfree(sg.v4, st);
+  tfree(sg.ix, st);
+}
+
+void check_reset(UploadCheck& h) {
   for (int a = 0; a < 3; ++a) {
     h.lo[a] = FLT_MAX;
     h.hi[a] = -FLT_MAX;
   }
+  h.rmax = 0.0f;
   h.bad = ~0ull;
+  h.bad_tri = ~0ull;
+}
+
+// Copies n discs to the device, converts and checks them; the verdict is
+// read back (one synchronisation).  Leaves the context untouched.
+int stage_discs(rtg_context* ctx, const float* pts, const float* nrm, const float* rad, int64_t n, Staged& sg) {
+  if (n < 0 || (n > 0 && (!pts || !nrm || !rad)))
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "discs: null array or negative count");
+  cudaStream_t st = ctx->stream;
+  sg.discs = true;
+  sg.nd = n;
+  check_reset(sg.hd);
+  if (n == 0) return RTG_OK;
   DBuf<float> raw;
-  DBuf<float4> cr, nn;
   DBuf<UploadCheck> chk;
-  int rc = RTG_OK;
-  if (n > 0) {
-    rc = talloc(ctx, raw, (size_t)(7 * n), st, "disc upload");
-    if (rc == RTG_OK) rc = talloc(ctx, cr, (size_t)n, st, "disc upload");
-    if (rc == RTG_OK) rc = talloc(ctx, nn, (size_t)n, st, "disc upload");
-    if (rc == RTG_OK) rc = talloc(ctx, chk, 1, st, "disc upload");
-    cudaError_t e = cudaSuccess;
-    if (rc == RTG_OK) e = cudaMemcpyAsync(raw.p, pts, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (rc == RTG_OK && e == cudaSuccess)
-      e = cudaMemcpyAsync(raw.p + 3 * n, nrm, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (rc == RTG_OK && e == cudaSuccess)
-      e = cudaMemcpyAsync(raw.p + 6 * n, rad, n * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (rc == RTG_OK && e == cudaSuccess) {
-      check_init_kernel<<<1, 1, 0, st>>>(chk.p);
-      disc_check_kernel<<<grid_for(n), 256, 0, st>>>(raw.p, raw.p + 3 * n, raw.p + 6 * n, n, cr.p, nn.p, chk.p);
-      e = cudaGetLastError();
-    }
-    if (rc == RTG_OK && e == cudaSuccess) e = cudaMemcpyAsync(&h, chk.p, sizeof h, cudaMemcpyDeviceToHost, st);
-    if (rc == RTG_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "disc upload");
-    if (rc == RTG_OK && h.bad != ~0ull) {  // the message of the first offending disc, as the host sees it
-      const int64_t i = (int64_t)h.bad;
-      const float* q = nrm + 3 * i;
-      const bool finite = finite3(pts + 3 * i) && finite3(q) && std::isfinite(rad[i]) && rad[i] > 0.0f;
-      rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
-                     "disc " + std::to_string(i) +
-                         (finite ? ": normal is not unit length" : ": non-finite value or radius <= 0"));
-    }
+  int rc = talloc(ctx, raw, (size_t)(7 * n), st, "disc upload");
+  if (rc == RTG_OK) rc = talloc(ctx, sg.cr, (size_t)n, st, "disc upload");
+  if (rc == RTG_OK) rc = talloc(ctx, sg.nn, (size_t)n, st, "disc upload");
+  if (rc == RTG_OK) rc = talloc(ctx, chk, 1, st, "disc upload");
+  cudaError_t e = cudaSuccess;
+  if (rc == RTG_OK) e = cudaMemcpyAsync(raw.p, pts, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (rc == RTG_OK && e == cudaSuccess)
+    e = cudaMemcpyAsync(raw.p + 3 * n, nrm, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (rc == RTG_OK && e == cudaSuccess)
+    e = cudaMemcpyAsync(raw.p + 6 * n, rad, n * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (rc == RTG_OK && e == cudaSuccess) {
+    check_init_kernel<<<1, 1, 0, st>>>(chk.p);
+    disc_check_kernel<<<grid_for(n), 256, 0, st>>>(raw.p, raw.p + 3 * n, raw.p + 6 * n, n, sg.cr.p, sg.nn.p,
+                                                      chk.p);
+    e = cudaGetLastError();
   }
-  if (rc == RTG_OK) {
-    g.nd = n;
-    for (int a = 0; a < 3; ++a) {
-      g.cmin[a] = h.lo[a];
-      g.cmax[a] = h.hi[a];
-    }
-    g.rmax = h.rmax;
-    rc = dalloc(ctx, g.disc_cr_by_id, (size_t)(n > 0 ? n : 1), "discs");
-    if (rc == RTG_OK) rc = dalloc(ctx, g.disc_n_by_id, (size_t)(n > 0 ? n : 1), "disc normals");
-    cudaError_t e = cudaSuccess;
-    if (rc == RTG_OK && n > 0)
-      e = cudaMemcpyAsync(g.disc_cr_by_id.p, cr.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-    if (rc == RTG_OK && n > 0 && e == cudaSuccess)
-      e = cudaMemcpyAsync(g.disc_n_by_id.p, nn.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "disc upload");
-  }
+  if (rc == RTG_OK && e == cudaSuccess) e = cudaMemcpyAsync(&sg.hd, chk.p, sizeof sg.hd, cudaMemcpyDeviceToHost, st);
+  if (rc == RTG_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "disc upload");
   tfree(raw, st);
-  tfree(cr, st);
-  tfree(nn, st);
   tfree(chk, st);
+  if (rc == RTG_OK && sg.hd.bad != ~0ull) {  // the message of the first offending disc, as the host sees it
+    const int64_t i = (int64_t)sg.hd.bad;
+    const float* q = nrm + 3 * i;
+    const bool finite = finite3(pts + 3 * i) && finite3(q) && std::isfinite(rad[i]) && rad[i] > 0.0f;
+    rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
+                   "disc " + std::to_string(i) +
+                       (finite ? ": normal is not unit length" : ": non-finite value or radius <= 0"));
+  }
   return rc;
 }
 
-int upload_triangles_impl(rtg_context* ctx, const float* vertices, const uint32_t* indices, int64_t nv,
-                          int64_t nt) {
+// The same for nv vertices and nt index triples.
+int stage_triangles(rtg_context* ctx, const float* vertices, const uint32_t* indices, int64_t nv, int64_t nt,
+                    Staged& sg) {
   if (nv < 0 || nt < 0 || (nt > 0 && (!vertices || !indices)) || (nv > 0 && !vertices))
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "triangles: null array or negative count");
+  cudaStream_t st = ctx->stream;
+  sg.triangles = true;
+  sg.nv = nv;
+  sg.nt = nt;
+  check_reset(sg.ht);
+  if (nv == 0 && nt == 0) return RTG_OK;
+  DBuf<float> raw;
+  DBuf<UploadCheck> chk;
+  int rc = talloc(ctx, chk, 1, st, "triangle upload");
+  if (rc == RTG_OK && nv > 0) rc = talloc(ctx, raw, (size_t)(3 * nv), st, "triangle upload");
+  if (rc == RTG_OK && nv > 0) rc = talloc(ctx, sg.v4, (size_t)nv, st, "triangle upload");
+  if (rc == RTG_OK && nt > 0) rc = talloc(ctx, sg.ix, (size_t)(3 * nt), st, "triangle upload");
+  cudaError_t e = cudaSuccess;
+  if (rc == RTG_OK && nv > 0) e = cudaMemcpyAsync(raw.p, vertices, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (rc == RTG_OK && nt > 0 && e == cudaSuccess)
+    e = cudaMemcpyAsync(sg.ix.p, indices, 3 * nt * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+  if (rc == RTG_OK && e == cudaSuccess) {
+    check_init_kernel<<<1, 1, 0, st>>>(chk.p);
+    if (nv > 0) vertex_check_kernel<<<grid_for(nv), 256, 0, st>>>(raw.p, nv, sg.v4.p, chk.p);
+    if (nt > 0) triangle_check_kernel<<<grid_for(nt), 256, 0, st>>>(sg.ix.p, nt, nv, sg.v4.p, chk.p);
+    e = cudaGetLastError();
+  }
+  if (rc == RTG_OK && e == cudaSuccess) e = cudaMemcpyAsync(&sg.ht, chk.p, sizeof sg.ht, cudaMemcpyDeviceToHost, st);
+  if (rc == RTG_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "triangle upload");
+  tfree(raw, st);
+  tfree(chk, st);
+  if (rc == RTG_OK && sg.ht.bad != ~0ull)
+    rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "vertex " + std::to_string(sg.ht.bad) + " is not finite");
+  else if (rc == RTG_OK && sg.ht.bad_tri != ~0ull)
+    rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
+                   "triangle " + std::to_string(sg.ht.bad_tri) + ": vertex index out of range");
+  return rc;
+}
+
+// Makes a checked upload the context's surface data (by id).
+int commit(rtg_context* ctx, const Staged& sg) {
   Geometry& g = ctx->g;
   cudaStream_t st = ctx->stream;
-  UploadCheck h{};
-  for (int a = 0; a < 3; ++a) {
-    h.lo[a] = FLT_MAX;
-    h.hi[a] = -FLT_MAX;
-  }
-  h.bad = ~0ull;
-  h.bad_tri = ~0ull;
-  DBuf<float> raw;
-  DBuf<float4> v4;
-  DBuf<uint32_t> ix;
-  DBuf<UploadCheck> chk;
-  int rc = RTG_OK;
-  if (nv > 0 || nt > 0) {
-    rc = talloc(ctx, chk, 1, st, "triangle upload");
-    if (rc == RTG_OK && nv > 0) rc = talloc(ctx, raw, (size_t)(3 * nv), st, "triangle upload");
-    if (rc == RTG_OK && nv > 0) rc = talloc(ctx, v4, (size_t)nv, st, "triangle upload");
-    if (rc == RTG_OK && nt > 0) rc = talloc(ctx, ix, (size_t)(3 * nt), st, "triangle upload");
-    cudaError_t e = cudaSuccess;
-    if (rc == RTG_OK && nv > 0) e = cudaMemcpyAsync(raw.p, vertices, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (rc == RTG_OK && nt > 0 && e == cudaSuccess)
-      e = cudaMemcpyAsync(ix.p, indices, 3 * nt * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-    if (rc == RTG_OK && e == cudaSuccess) {
-      check_init_kernel<<<1, 1, 0, st>>>(chk.p);
-      if (nv > 0) vertex_check_kernel<<<grid_for(nv), 256, 0, st>>>(raw.p, nv, v4.p, chk.p);
-      if (nt > 0) triangle_check_kernel<<<grid_for(nt), 256, 0, st>>>(ix.p, nt, nv, v4.p, chk.p);
-      e = cudaGetLastError();
-    }
-    if (rc == RTG_OK && e == cudaSuccess) e = cudaMemcpyAsync(&h, chk.p, sizeof h, cudaMemcpyDeviceToHost, st);
-    if (rc == RTG_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "triangle upload");
-    if (rc == RTG_OK && h.bad != ~0ull)
-      rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "vertex " + std::to_string(h.bad) + " is not finite");
-    else if (rc == RTG_OK && h.bad_tri != ~0ull)
-      rc = set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
-                     "triangle " + std::to_string(h.bad_tri) + ": vertex index out of range");
-  }
-  if (rc == RTG_OK) {
-    g.nt = nt;
-    g.nv = nv;
+  if (sg.discs) {
+    const int64_t n = sg.nd;
+    g.nd = n;
     for (int a = 0; a < 3; ++a) {
-      g.tri_min[a] = h.lo[a];
-      g.tri_max[a] = h.hi[a];
+      g.cmin[a] = sg.hd.lo[a];
+      g.cmax[a] = sg.hd.hi[a];
     }
-    rc = dalloc(ctx, g.tri_v, (size_t)(nv > 0 ? nv : 1), "vertices");
-    if (rc == RTG_OK) rc = dalloc(ctx, g.tri_idx, (size_t)(3 * (nt > 0 ? nt : 1)), "triangle indices");
-    cudaError_t e = cudaSuccess;
-    if (rc == RTG_OK && nv > 0) e = cudaMemcpyAsync(g.tri_v.p, v4.p, nv * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-    if (rc == RTG_OK && nt > 0 && e == cudaSuccess)
-      e = cudaMemcpyAsync(g.tri_idx.p, ix.p, 3 * nt * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
-    if (rc == RTG_OK && e != cudaSuccess) rc = check_cuda(ctx, e, "triangle upload");
+    g.rmax = sg.hd.rmax;
+    RTG_TRY(dalloc(ctx, g.disc_cr_by_id, (size_t)(n > 0 ? n : 1), "discs"));
+    RTG_TRY(dalloc(ctx, g.disc_n_by_id, (size_t)(n > 0 ? n : 1), "disc normals"));
+    if (n > 0) {
+      RTG_CUDA(ctx, cudaMemcpyAsync(g.disc_cr_by_id.p, sg.cr.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+      RTG_CUDA(ctx, cudaMemcpyAsync(g.disc_n_by_id.p, sg.nn.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    }
   }
-  tfree(raw, st);
-  tfree(v4, st);
-  tfree(ix, st);
-  tfree(chk, st);
-  return rc;
+  if (sg.triangles) {
+    g.nt = sg.nt;
+    g.nv = sg.nv;
+    for (int a = 0; a < 3; ++a) {
+      g.tri_min[a] = sg.ht.lo[a];
+      g.tri_max[a] = sg.ht.hi[a];
+    }
+    RTG_TRY(dalloc(ctx, g.tri_v, (size_t)(sg.nv > 0 ? sg.nv : 1), "vertices"));
+    RTG_TRY(dalloc(ctx, g.tri_idx, (size_t)(3 * (sg.nt > 0 ? sg.nt : 1)), "triangle indices"));
+    if (sg.nv > 0)
+      RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_v.p, sg.v4.p, sg.nv * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    if (sg.nt > 0)
+      RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_idx.p, sg.ix.p, 3 * sg.nt * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+  }
+  return RTG_OK;
 }
 
 }  // namespace
@@ -510,9 +523,14 @@ int rtg_upload_mixed(rtg_context* ctx, const float* points, const float* normals
                      const float* vertices, const uint32_t* indices, int64_t nv, int64_t nt) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   RTG_TRY(use_device(ctx));
-  RTG_TRY(upload_discs_impl(ctx, points, normals, radii, nd, true));
-  RTG_TRY(upload_triangles_impl(ctx, vertices, indices, nv, nt));
-  if (ctx->g.nd + ctx->g.nt == 0) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no primitives");
+  // both halves are checked before either replaces the context's surface
+  Staged sg;
+  int rc = stage_discs(ctx, points, normals, radii, nd, sg);
+  if (rc == RTG_OK) rc = stage_triangles(ctx, vertices, indices, nv, nt, sg);
+  if (rc == RTG_OK && nd + nt == 0) rc = set_error(ctx, RTG_ERR_NO_GEOMETRY, "no primitives");
+  if (rc == RTG_OK) rc = commit(ctx, sg);
+  release(sg, ctx->stream);
+  RTG_TRY(rc);
   dfree(ctx->sticking_field);
   return rebuild_all(ctx);
 }
@@ -529,7 +547,13 @@ int rtg_update_discs(rtg_context* ctx, const float* points, const float* normals
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   if (ctx->g.nd == 0 || !ctx->g.nodes.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no discs to update");
   RTG_TRY(use_device(ctx));
-  RTG_TRY(upload_discs_impl(ctx, points, normals, radii, n, false));
+  if (n != ctx->g.nd)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "update_discs: the disc count must not change");
+  Staged sg;
+  int rc = stage_discs(ctx, points, normals, radii, n, sg);
+  if (rc == RTG_OK) rc = commit(ctx, sg);
+  release(sg, ctx->stream);
+  RTG_TRY(rc);
   RTG_TRY(refit_lbvh(ctx));
   RTG_TRY(build_neighbors(ctx));
   RTG_TRY(alloc_results(ctx));

@@ -106,3 +106,27 @@ def test_invalid_inputs_are_refused(eng):
         eng.configure(sticking=2.0)
     with pytest.raises(RtgError, match="roulette"):
         eng.configure(roulette_threshold=0.5, roulette_weight=0.3)
+
+
+def test_refused_upload_keeps_the_surface(eng):
+    """A refused upload (of either half of a mixed surface) leaves the previous
+    surface as it was: the same trace gives the same hits afterwards."""
+    from rti_gb300 import RtgError
+    from rti_gb300 import scenes
+    t = scenes.trench_discs(domain=1.2, width=0.4, depth=1.0)
+    eng.upload_discs(t.points, t.normals, t.radii)
+    eng.configure(box=(t.box_lo, t.box_hi), x_bound=1, y_bound=1, sticking=0.1, reset=True)
+    eng.trace(50000, 3)
+    before = eng.hit_counts()
+    v = np.zeros((3, 3), np.float32)
+    with pytest.raises(RtgError, match="out of range"):
+        eng.upload_triangles(v, np.uint32([[0, 1, 3]]))
+    with pytest.raises(RtgError, match="out of range"):
+        eng.upload_mixed(t.points, t.normals, t.radii, v, np.uint32([[0, 1, 7]]))
+    bad = t.points.copy()
+    bad[5, 2] = np.nan
+    with pytest.raises(RtgError, match="non-finite"):
+        eng.upload_discs(bad, t.normals, t.radii)
+    assert eng.num_primitives == t.n
+    eng.trace(50000, 3)
+    assert np.array_equal(eng.hit_counts(), before)
