@@ -573,6 +573,7 @@ def main():
     ap.add_argument("--sweep", default="", help="comma-separated ray counts: path-kernel time against rays "
                                                 "(the tail analysis), printed instead of the bench line")
     ap.add_argument("--rough-rays", type=int, default=100_000_000, help="rays of the rough-surface block")
+    ap.add_argument("--rough-only", action="store_true", help="run the rough-surface block alone and print it")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     from __graft_entry__ import build
@@ -580,6 +581,9 @@ def main():
         from oracle import oracle
         oracle.build()
         run_reference(args)
+    elif args.rough_only:
+        build()
+        print(json.dumps(run_rough_block(args)))
     else:
         build()
         run_ours(args)
