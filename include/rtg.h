@@ -152,7 +152,9 @@ RTG_API const char* rtg_last_error(const rtg_context* ctx);
 /* points: n x 3 centres, normals: n x 3 unit normals, radii: n (rti's "grid
  * spacing", used as the disc radius, device.hpp:213-216).  Builds the LBVH and
  * the neighbour lists.  Replaces any previous geometry; clears the sticking
- * field. */
+ * field.  The arrays are checked on the device before anything is replaced:
+ * a refused upload (non-finite value, radius <= 0, normal not of unit length,
+ * index out of range) leaves the previous surface as it was. */
 RTG_API int rtg_upload_discs(rtg_context* ctx, const float* points, const float* normals, const float* radii,
                      int64_t n);
 /* vertices: nv x 3, indices: nt x 3 (uint32).  Replaces any previous geometry. */
