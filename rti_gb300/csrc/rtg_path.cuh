@@ -4,17 +4,19 @@
 // One thread carries one particle path at a time, as tracer::run does per
 // OpenMP iteration (tracer.hpp:160-280): source ray, closest hit, periodic or
 // reflective x/y box, back-face pass-through, sticking deposit on the hit
-// primitive and on every crossed overlapping neighbour disc, Russian
-// roulette, diffuse/specular re-emission.  Threads are persistent: when at
+// primitive and on every crossed overlapping neighbour disc (kModeWindow: on
+// every disc met in the multi-hit window instead), Russian roulette,
+// diffuse/specular re-emission.  Threads are persistent: when at
 // least `packet` lanes of a warp are idle, the warp takes that many next
 // source-ray ids from a global counter (one atomic per warp), so long and
 // short paths share the SIMD lanes.
 //
 // Closest hit = stack traversal of the two-box LBVH nodes; ties in t go to the
 // lower primitive id, and the node boxes are conservative, so the chosen hit
-// does not depend on the traversal order.  The stack holds STACK entries; a
-// tree deeper than that would overflow it (counted as an error), so the host
-// picks STACK from the tree depth.
+// does not depend on the traversal order.  The stack holds STACK entries (in
+// local memory, or in shared memory with one column per thread); a tree
+// deeper than that would overflow it (counted as an error), so the host picks
+// STACK from the tree depth.
 #pragma once
 #include <cfloat>
 #include <climits>
