@@ -243,6 +243,25 @@ def test_refit_after_move_equals_fresh_upload(eng, trench, oracle_lib):
     assert a["tally"].segments == b["tally"].segments
 
 
+def test_vertex_update_equals_fresh_upload(eng, hole):
+    """Moved triangle vertices (rtg_update_vertices: refit, same topology) trace
+    like a fresh upload of the moved mesh, and a refused update is reported."""
+    from rti_gb300 import RtgError
+    eng.upload_triangles(hole.vertices, hole.indices)
+    moved = hole.vertices.copy()
+    moved[:, 2] += (0.002 * np.cos(moved[:, 1] * 5)).astype(np.float32)
+    eng.update_vertices(moved)
+    eng.configure(box=(hole.box_lo, hole.box_hi), sticking=0.01, x_bound=1, y_bound=1, reset=True)
+    a = _gpu_trace(eng, 50000, seed=6)
+    with pytest.raises(RtgError):
+        eng.update_vertices(moved[:-1])
+    eng.upload_triangles(moved, hole.indices)
+    eng.configure(box=(hole.box_lo, hole.box_hi), sticking=0.01, x_bound=1, y_bound=1, reset=True)
+    b = _gpu_trace(eng, 50000, seed=6)
+    assert np.array_equal(a["counts"], b["counts"])
+    assert a["tally"].segments == b["tally"].segments
+
+
 def test_abort_returns_status(eng, trench):
     from rti_gb300 import RtgError
     _upload_discs(eng, trench, sticking=0.001, x_bound=1, y_bound=1)
