@@ -98,6 +98,17 @@ def test_wavefront_truncation_field_and_reflective_box(eng):
     eng.set_launch_config()
 
 
+def test_invalid_launch_configs_are_refused(eng):
+    from rti_gb300 import RtgError
+    _trench(eng)
+    for kw, msg in ((dict(threads_per_block=96), "threads_per_block"), (dict(packet=0), "packet"),
+                    (dict(stack_depth=48), "stack_depth"), (dict(scheduling=7), "scheduling"),
+                    (dict(leaf_tests=3), "leaf_tests"), (dict(stack_memory=5), "stack_memory")):
+        with pytest.raises(RtgError, match=msg):
+            eng.set_launch_config(**kw)
+    eng.set_launch_config()
+
+
 def test_autotune_picks_a_valid_config_and_results_stay(eng):
     _hole(eng)
     eng.set_launch_config()

@@ -118,3 +118,5 @@ def test_window_plain_schedule_and_refusals(eng, oracle_lib):
     b.close()
     with pytest.raises(RtgError, match="window_factor"):
         eng.set_deposit_mode(1, -1.0)
+    with pytest.raises(RtgError, match="mode must be"):
+        eng.set_deposit_mode(7, 5.0)
