@@ -176,6 +176,47 @@ def hole_triangles(radius: float = 0.5, depth: float = 10.0, cell: float = 2.0, 
                                           "n_theta": n_theta, "n_wall": n_wall, "jitter": jitter, "seed": seed})
 
 
+def trench_triangles(width: float = 1.0, depth: float = 5.0, cell: float = 3.0, n_wall: int = 50,
+                     n_bottom: int = 20, n_top: int = 4, n_y: int = 6, source_gap: float = 0.1) -> TriangleSurface:
+    """A rectangular trench along y (infinite through the periodic cell) as a
+    triangle mesh, every face wound so that its normal points into the open
+    space: flat top on both sides (z = 0), walls of n_wall bands in depth,
+    bottom of n_bottom strips across.  Primitive order: top, left wall (bands
+    from the top down), bottom (strips left to right), right wall (bands from
+    the top down), n_y pieces along y in each, two triangles per quad."""
+    x0 = (cell - width) / 2.0
+    x1 = x0 + width
+    ys = np.linspace(0.0, cell, n_y + 1)
+    V, T = [], []
+
+    def quad(p00, p10, p11, p01):  # counter-clockwise seen from the side the normal points to
+        b = len(V)
+        V.extend([p00, p10, p11, p01])
+        T.extend([(b, b + 1, b + 2), (b, b + 2, b + 3)])
+
+    for xa, xb in list(zip(np.linspace(0.0, x0, n_top + 1)[:-1], np.linspace(0.0, x0, n_top + 1)[1:])) + \
+            list(zip(np.linspace(x1, cell, n_top + 1)[:-1], np.linspace(x1, cell, n_top + 1)[1:])):
+        for ya, yb in zip(ys[:-1], ys[1:]):  # top, normal +z
+            quad((xa, ya, 0.0), (xb, ya, 0.0), (xb, yb, 0.0), (xa, yb, 0.0))
+    zs = np.linspace(0.0, -depth, n_wall + 1)
+    for za, zb in zip(zs[:-1], zs[1:]):
+        for ya, yb in zip(ys[:-1], ys[1:]):  # left wall at x0, normal +x
+            quad((x0, ya, zb), (x0, yb, zb), (x0, yb, za), (x0, ya, za))
+    xs = np.linspace(x0, x1, n_bottom + 1)
+    for xa, xb in zip(xs[:-1], xs[1:]):
+        for ya, yb in zip(ys[:-1], ys[1:]):  # bottom, normal +z
+            quad((xa, ya, -depth), (xb, ya, -depth), (xb, yb, -depth), (xa, yb, -depth))
+    for za, zb in zip(zs[:-1], zs[1:]):
+        for ya, yb in zip(ys[:-1], ys[1:]):  # right wall at x1, normal -x
+            quad((x1, ya, zb), (x1, ya, za), (x1, yb, za), (x1, yb, zb))
+    V = _f32(np.array(V))
+    T = np.array(T, dtype=np.uint32)
+    lo = (0.0, 0.0, float(-depth))
+    hi = (float(np.float32(cell)), float(np.float32(cell)), float(np.float32(source_gap)))
+    return TriangleSurface(V, T, lo, hi, {"kind": "trench", "width": width, "depth": depth, "cell": cell,
+                                          "n_wall": n_wall, "n_bottom": n_bottom, "n_top": n_top, "n_y": n_y})
+
+
 def triangle_normals(V: np.ndarray, T: np.ndarray) -> np.ndarray:
     e1 = V[T[:, 1]].astype(np.float64) - V[T[:, 0]]
     e2 = V[T[:, 2]].astype(np.float64) - V[T[:, 0]]
