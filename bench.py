@@ -202,9 +202,31 @@ def run_reference(args):
             "impl": "reference", "config": config_dict(h, sample),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{sample} source rays of the workload per step, all host threads; "
-                                       "C restatement of rti's tracer (rti's Embree path does not build here)"},
+                                       "C restatement of rti's tracer (rti's Embree path does not build here)",
+                             "host": host_info()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def host_info() -> dict:
+    """The host CPU the baseline ran on: model, ISA, logical cores."""
+    import platform
+    model = platform.processor() or ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu part", "hardware") and not model:
+                    model = line.split(":", 1)[1].strip()
+                if key == "model name":
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return {"cpu_model": model or "unknown", "isa": platform.machine(), "nproc": os.cpu_count(),
+            "build": "gcc -O3 -ffp-contract=off, OpenMP (oracle/Makefile)",
+            "note": "C restatement of rti's tracer; rti's Embree path does not build here "
+                    "(Embree 3.11 / VTK absent, x86-only intrinsics)"}
 
 
 class _CAI:
@@ -529,7 +551,8 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         rays_s, _ = cpu_sample(h, args.cpu_rays, os.cpu_count() or 1)
         cpu = {"value": rays_s, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{args.cpu_rays} source rays of the same workload, all host threads"}
+               "sample": f"{args.cpu_rays} source rays of the same workload, all host threads",
+               "host": host_info()}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
