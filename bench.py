@@ -211,18 +211,24 @@ def run_reference(args):
 def host_info() -> dict:
     """The host CPU the baseline ran on: model, ISA, logical cores."""
     import platform
-    model = platform.processor() or ""
-    try:
-        with open("/proc/cpuinfo") as f:
-            for line in f:
-                key = line.split(":")[0].strip().lower()
-                if key in ("model name", "cpu part", "hardware") and not model:
-                    model = line.split(":", 1)[1].strip()
-                if key == "model name":
-                    model = line.split(":", 1)[1].strip()
-                    break
-    except OSError:
+    model = ""
+    try:  # lscpu names Arm cores too ("Neoverse-V2"); /proc/cpuinfo has no model name there
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
         pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith("model name"):
+                        model = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
     return {"cpu_model": model or "unknown", "isa": platform.machine(), "nproc": os.cpu_count(),
             "build": "gcc -O3 -ffp-contract=off, OpenMP (oracle/Makefile)",
             "note": "C restatement of rti's tracer; rti's Embree path does not build here "
