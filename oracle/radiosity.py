@@ -10,7 +10,8 @@ incoming flux density G_i on patch i obeys
 
 with F the patch-to-patch view factors; E0 = 1 is the flux density through the
 opening plane (the flux density on the flat top surface of the Monte Carlo
-scenes).  rti ships radiosity data only for one cylinder (verification/
+scenes).  Both solvers also return dG/ds, the exact derivative of the solution
+with respect to a global sticking (what an unbiased adjoint estimates).  rti ships radiosity data only for one cylinder (verification/
 radiosity/analytical_solution: radius 0.5, length 45); these solvers give the
 same for any cylindrical hole and for an infinite trench, and are checked
 against that data first.
@@ -31,6 +32,14 @@ against that data first.
 from __future__ import annotations
 
 import numpy as np
+
+
+def _solve(F, f_open, s):
+    """G = (I - (1 - s) F)^-1 f_open and its derivative with respect to the
+    sticking s, dG/ds = -(I - (1 - s) F)^-1 F G."""
+    A = np.eye(len(f_open)) - (1.0 - s) * F
+    G = np.linalg.solve(A, f_open)
+    return G, np.linalg.solve(A, -(F @ G))
 
 
 def disc_to_disc(r1, r2, h):
@@ -79,9 +88,9 @@ def hole(radius: float, depth: float, sticking: float, n_wall: int = 400, n_bott
     F[nw:, :nw] = sec[:, 1:] - sec[:, :-1]
     F[:nw, nw:] = (F[nw:, :nw] * area[nw:, None] / area[None, :nw]).T
     f_open[nw:] = sec[:, 0]
-    G = np.linalg.solve(np.eye(n) - (1.0 - s) * F, f_open)
-    return {"wall_depth": 0.5 * (zw[1:] + zw[:-1]), "wall": G[:nw],
-            "bottom_radius": 0.5 * (rb[1:] + rb[:-1]), "bottom": G[nw:],
+    G, dG = _solve(F, f_open, s)
+    return {"wall_depth": 0.5 * (zw[1:] + zw[:-1]), "wall": G[:nw], "d_wall": dG[:nw],
+            "bottom_radius": 0.5 * (rb[1:] + rb[:-1]), "bottom": G[nw:], "d_bottom": dG[nw:],
             "direct_wall": f_open[:nw], "direct_bottom": f_open[nw:], "row_sums": F.sum(1) + f_open}
 
 
@@ -121,7 +130,8 @@ def trench(width: float, depth: float, sticking: float, n_wall: int = 200, n_bot
             if not same_line:
                 F[i, j] = _strings(p, q, u, v) / (2.0 * L[i])
         f_open[i] = _strings(p, q, opening[0], opening[1]) / (2.0 * L[i])
-    G = np.linalg.solve(np.eye(n) - (1.0 - s) * F, f_open)
-    return {"wall_depth": 0.5 * (zw[1:] + zw[:-1]), "wall": G[:n_wall],
+    G, dG = _solve(F, f_open, s)
+    return {"wall_depth": 0.5 * (zw[1:] + zw[:-1]), "wall": G[:n_wall], "d_wall": dG[:n_wall],
             "bottom_x": 0.5 * (xb[1:] + xb[:-1]), "bottom": G[n_wall:n_wall + n_bottom],
+            "d_bottom": dG[n_wall:n_wall + n_bottom],
             "right_wall": G[n_wall + n_bottom:][::-1], "row_sums": F.sum(1) + f_open}

@@ -148,3 +148,48 @@ def test_disc_trench_near_radiosity(rtg_lib):
     err = np.linalg.norm(sim - ref) / np.linalg.norm(ref)
     print(f"disc trench s={s}: wall L2 {err:.4f}, mean ratio {np.mean(sim / ref):.4f}")
     assert err < 0.05
+
+
+@pytest.mark.parametrize("shape", ["trench", "hole"])
+def test_unbiased_adjoint_matches_radiosity_derivative(rtg_lib, shape):
+    """dL/ds of the flux L onto a target region (trench bottom, or the lowest
+    quarter of an AR-10 hole's wall) by the unbiased adjoint replay, against
+    the exact derivative of the radiosity solution, sum over the region of
+    A_i (G_i + s dG_i/ds); the forward L against sum of s G_i A_i."""
+    from rti_gb300 import Engine
+    from oracle import radiosity as RD
+    s, n = 0.1, 10_000_000
+    if shape == "trench":
+        surf = scenes.trench_triangles(width=1.0, depth=5.0, cell=3.0, n_wall=50, n_bottom=20, n_top=4, n_y=6)
+        V, T = surf.vertices, surf.indices
+        c = V.astype(np.float64)[T].mean(axis=1)
+        q = np.abs(c[:, 2] + 5.0) < 1e-6
+        sol = RD.trench(1.0, 5.0, s, n_wall=250, n_bottom=100)
+        strip = np.clip(((c[:, 0] - 1.0) / 0.05).astype(int), 0, 19)
+        G = sol["bottom"].reshape(20, 5).mean(1)[strip]
+        dG = sol["d_bottom"].reshape(20, 5).mean(1)[strip]
+    else:
+        surf = scenes.cylinder_triangles(radius=0.5, depth=10.0, cell=2.0, n_theta=128, n_wall=200, n_top=8,
+                                         n_bottom=8)
+        V, T = surf.vertices, surf.indices
+        c = V.astype(np.float64)[T].mean(axis=1)
+        q = (c[:, 2] < -7.5) & (c[:, 2] > -10.0 + 1e-6)
+        sol = RD.hole(0.5, 10.0, s, n_wall=1000, n_bottom=40)
+        band = np.clip((-c[:, 2] / 0.05).astype(int), 0, 199)
+        G = sol["wall"].reshape(200, 5).mean(1)[band]
+        dG = sol["d_wall"].reshape(200, 5).mean(1)[band]
+    area = _areas(V, T)
+    cell = (surf.box_hi[0] - surf.box_lo[0]) * (surf.box_hi[1] - surf.box_lo[1])
+    g = q.astype(np.float64)
+    with Engine(0) as e:
+        e.upload_triangles(V, T)
+        e.configure(box=(surf.box_lo, surf.box_hi), sticking=s, x_bound=1, y_bound=1, reflection=0)
+        e.trace(n, seed=8)
+        L = float(np.dot(g, e.values())) / (n / cell)
+        ds, _, _ = e.adjoint(g, n, seed=8, unbiased=True)
+    ds /= n / cell
+    L_ref = float(np.sum((s * G * area)[q]))
+    ds_ref = float(np.sum((area * (G + s * dG))[q]))
+    print(f"{shape}: L {L:.5f} vs {L_ref:.5f}; dL/ds {ds:.5f} vs {ds_ref:.5f}")
+    assert abs(L / L_ref - 1.0) < 0.01
+    assert abs(ds / ds_ref - 1.0) < 0.03
