@@ -101,12 +101,10 @@ def _strings(p, q, u, v):
     return abs((d(p, v) + d(q, u)) - (d(p, u) + d(q, v)))
 
 
-def trench(width: float, depth: float, sticking: float, n_wall: int = 200, n_bottom: int = 100):
-    """Radiosity of an infinitely long rectangular trench (cross-section in the
-    x-z plane, opening at z = 0 between x = 0 and x = width).  Returns the left
-    wall strip centres (depth), the bottom strip centres (x) and their incoming
-    flux densities G (the right wall mirrors the left)."""
-    W, D, s = float(width), float(depth), float(sticking)
+def _trench_system(W, D, n_wall, n_bottom):
+    """Strips of the trench cross-section (left wall top-down, bottom left to
+    right, right wall bottom-up), their lengths, view factors and view factors
+    to the opening."""
     zw = np.linspace(0.0, D, n_wall + 1)
     xb = np.linspace(0.0, W, n_bottom + 1)
     segs = []  # each strip as its two end points
@@ -130,8 +128,43 @@ def trench(width: float, depth: float, sticking: float, n_wall: int = 200, n_bot
             if not same_line:
                 F[i, j] = _strings(p, q, u, v) / (2.0 * L[i])
         f_open[i] = _strings(p, q, opening[0], opening[1]) / (2.0 * L[i])
-    G, dG = _solve(F, f_open, s)
+    return zw, xb, L, F, f_open
+
+
+def trench(width: float, depth: float, sticking: float, n_wall: int = 200, n_bottom: int = 100):
+    """Radiosity of an infinitely long rectangular trench (cross-section in the
+    x-z plane, opening at z = 0 between x = 0 and x = width).  Returns the left
+    wall strip centres (depth), the bottom strip centres (x) and their incoming
+    flux densities G and dG/ds (the right wall mirrors the left)."""
+    zw, xb, L, F, f_open = _trench_system(float(width), float(depth), n_wall, n_bottom)
+    G, dG = _solve(F, f_open, float(sticking))
     return {"wall_depth": 0.5 * (zw[1:] + zw[:-1]), "wall": G[:n_wall], "d_wall": dG[:n_wall],
             "bottom_x": 0.5 * (xb[1:] + xb[:-1]), "bottom": G[n_wall:n_wall + n_bottom],
             "d_bottom": dG[n_wall:n_wall + n_bottom],
             "right_wall": G[n_wall + n_bottom:][::-1], "row_sums": F.sum(1) + f_open}
+
+
+def trench_field_gradient(width: float, depth: float, sticking, n_wall: int, n_bottom: int,
+                          length: float = 1.0, target: str = "bottom"):
+    """Per-strip sticking sigma (a scalar or one value per strip, in the strip
+    order of the cross-section: left wall top-down, bottom, right wall
+    bottom-up) and L = sum over the target strips of sigma_i G_i A_i (A_i =
+    strip length x `length`): returns L and dL/dsigma_j for every strip, from
+    G = f + F diag(1 - sigma) G and one adjoint solve,
+        dL/dsigma_j = [j in target] A_j G_j - lambda^T F[:, j] G_j,
+        lambda = (I - F diag(1 - sigma))^-T (sigma A [target])."""
+    zw, xb, Ls, F, f_open = _trench_system(float(width), float(depth), n_wall, n_bottom)
+    n = len(f_open)
+    sigma = np.broadcast_to(np.asarray(sticking, dtype=np.float64), (n,)).copy()
+    area = Ls * float(length)
+    q = np.zeros(n)
+    if target == "bottom":
+        q[n_wall:n_wall + n_bottom] = 1.0
+    else:
+        raise ValueError("target must be 'bottom'")
+    M = np.eye(n) - F * (1.0 - sigma)[None, :]
+    G = np.linalg.solve(M, f_open)
+    w = sigma * area * q
+    lam = np.linalg.solve(M.T, w)
+    grad = q * area * G - (lam @ F) * G
+    return {"L": float(w @ G), "grad": grad, "n_wall": n_wall, "n_bottom": n_bottom}

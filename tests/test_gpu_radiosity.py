@@ -193,3 +193,36 @@ def test_unbiased_adjoint_matches_radiosity_derivative(rtg_lib, shape):
     print(f"{shape}: L {L:.5f} vs {L_ref:.5f}; dL/ds {ds:.5f} vs {ds_ref:.5f}")
     assert abs(L / L_ref - 1.0) < 0.01
     assert abs(ds / ds_ref - 1.0) < 0.03
+
+
+def test_field_adjoint_matches_radiosity_gradient(rtg_lib):
+    """dL/ds_j of the flux onto the trench bottom with respect to the sticking
+    of each wall band and bottom strip (the per-primitive field gradients of
+    the unbiased adjoint replay, summed over the triangles of a strip) against
+    the exact radiosity gradient for a per-strip sticking."""
+    from rti_gb300 import Engine
+    from oracle import radiosity as RD
+    s, n, nw, nb = 0.1, 10_000_000, 50, 20
+    surf = scenes.trench_triangles(width=1.0, depth=5.0, cell=3.0, n_wall=nw, n_bottom=nb, n_top=4, n_y=6)
+    V, T = surf.vertices, surf.indices
+    c = V.astype(np.float64)[T].mean(axis=1)
+    left, right = np.abs(c[:, 0] - 1.0) < 1e-6, np.abs(c[:, 0] - 2.0) < 1e-6
+    bottom = np.abs(c[:, 2] + 5.0) < 1e-6
+    # strip of every cavity triangle in the solver's order: left wall top-down, bottom, right wall bottom-up
+    strip = np.full(len(T), -1)
+    strip[left] = np.clip((-c[left, 2] / 0.1).astype(int), 0, nw - 1)
+    strip[bottom] = nw + np.clip(((c[bottom, 0] - 1.0) / 0.05).astype(int), 0, nb - 1)
+    strip[right] = nw + nb + (nw - 1 - np.clip((-c[right, 2] / 0.1).astype(int), 0, nw - 1))
+    cell = (surf.box_hi[0] - surf.box_lo[0]) * (surf.box_hi[1] - surf.box_lo[1])
+    with Engine(0) as e:
+        e.upload_triangles(V, T)
+        e.configure(box=(surf.box_lo, surf.box_hi), x_bound=1, y_bound=1, reflection=0)
+        e.set_sticking_field(np.full(len(T), s, np.float32))
+        _, _, field = e.adjoint(bottom.astype(np.float64), n, seed=12, unbiased=True)
+    inside = strip >= 0
+    sim = np.bincount(strip[inside], weights=field[inside], minlength=2 * nw + nb) / (n / cell)
+    ref = RD.trench_field_gradient(1.0, 5.0, s, nw, nb, length=surf.box_hi[1] - surf.box_lo[1])["grad"]
+    err = np.linalg.norm(sim - ref) / np.linalg.norm(ref)
+    print(f"field gradient L2 {err:.4f}; bottom strip {sim[nw + 10]:.5f} vs {ref[nw + 10]:.5f}, "
+          f"top wall band {sim[0]:.5f} vs {ref[0]:.5f}")
+    assert err < 0.05
