@@ -98,3 +98,23 @@ def test_oracle_trench_matches_radiosity(oracle_lib):
     ref = RD.trench(1.0, 5.0, s, n_wall=100, n_bottom=50)["wall"].reshape(10, 10).mean(1)
     err = np.linalg.norm(sim - ref) / np.linalg.norm(ref)
     assert err < 0.04, (err, sim, ref)
+
+
+def test_radiosity_derivatives_match_differences():
+    """dG/ds of both solvers and the per-strip field gradient of the trench
+    against central differences of the solutions themselves."""
+    from oracle import radiosity as RD
+    h = 1e-6
+    for solve in (lambda s: RD.trench(1.0, 5.0, s, 60, 20), lambda s: RD.hole(0.5, 10.0, s, 200, 20)):
+        a, p, m = solve(0.1), solve(0.1 + h), solve(0.1 - h)
+        fd = (p["wall"] - m["wall"]) / (2 * h)
+        assert np.max(np.abs(fd - a["d_wall"])) < 1e-7 * np.max(np.abs(a["d_wall"])) + 1e-9
+    r = RD.trench_field_gradient(1.0, 5.0, 0.1, 20, 10, length=3.0)
+    sig = np.full(50, 0.1)
+    for j in (0, 7, 19, 20, 24, 29, 30, 49):
+        sp, sm = sig.copy(), sig.copy()
+        sp[j] += h
+        sm[j] -= h
+        fd = (RD.trench_field_gradient(1.0, 5.0, sp, 20, 10, 3.0)["L"] -
+              RD.trench_field_gradient(1.0, 5.0, sm, 20, 10, 3.0)["L"]) / (2 * h)
+        assert abs(fd - r["grad"][j]) < 1e-7 * np.max(np.abs(r["grad"])), (j, fd, r["grad"][j])
