@@ -217,6 +217,18 @@ RTG_API int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder);
 #define RTG_DEPOSIT_WINDOW 1
 RTG_API int rtg_set_deposit_mode(rtg_context* ctx, int32_t mode, float window_factor);
 RTG_API int rtg_get_deposit_mode(const rtg_context* ctx, int32_t* mode, float* window_factor);
+/* How the flux S1 is summed during a trace (S2..S4 are always FP64):
+ *   RTG_ACCUM_FP64 (default): FP64 atomics, as rti's double accumulators; the
+ *     last bits of a sum depend on the order of the atomics;
+ *   RTG_ACCUM_FIXED: every deposit rounded to a multiple of 2^-32 and summed
+ *     in 64-bit integers, converted to double when the trace ends: the sums do
+ *     not depend on the order, so repeated traces (and sharded ones summed in
+ *     any order) give the same S1 bit for bit.  Up to 2^31 per primitive.
+ * Single traces of a context (a batch refuses a context in fixed mode). */
+#define RTG_ACCUM_FP64 0
+#define RTG_ACCUM_FIXED 1
+RTG_API int rtg_set_accumulation(rtg_context* ctx, int32_t mode);
+RTG_API int rtg_get_accumulation(const rtg_context* ctx, int32_t* mode);
 /* Autotuner: for each tree builder (RTG_TREE_*), times each candidate launch
  * configuration (block size x packet x stack depth x scheduling) on source
  * rays [0, sample_rays) with `seed` under the current surface and

@@ -45,6 +45,7 @@ class OrcConfig(C.Structure):
         ("sticking_field", _f32p),
         ("window", C.c_int32),
         ("window_factor", C.c_float),
+        ("accum_fixed", C.c_int32),
     ]
 
 
@@ -263,7 +264,7 @@ def adjoint(scene: "Scene", cfg: OrcConfig, g, ray_begin: int, ray_end: int, nth
 
 def make_config(box_lo, box_hi, *, x_bound=1, y_bound=1, reflection=0, specular_fraction=0.0,
                 sticking=0.1, source_exponent=1.0, tnear=1e-4, max_segments=1 << 16, job=0, seed=0,
-                src_lo=None, src_hi=None, window=0, window_factor=5.0) -> OrcConfig:
+                src_lo=None, src_hi=None, window=0, window_factor=5.0, accum_fixed=0) -> OrcConfig:
     c = OrcConfig()
     c.x_bound, c.y_bound, c.reflection = x_bound, y_bound, reflection
     c.specular_fraction, c.sticking, c.source_exponent = specular_fraction, sticking, source_exponent
@@ -280,6 +281,7 @@ def make_config(box_lo, box_hi, *, x_bound=1, y_bound=1, reflection=0, specular_
     c.max_segments, c.job, c.seed = max_segments, job, seed
     c.sticking_field = None
     c.window, c.window_factor = window, window_factor
+    c.accum_fixed = accum_fixed
     return c
 
 

@@ -624,12 +624,21 @@ typedef struct {
   double *s1, *s2, *s3, *s4;
   uint64_t* cnt;
   orc_tally t;
+  int fixed; /* s1 holds int64 multiples of 2^-32 */
 } acc_t;
 
-/* hit_accumulator::use (hit_accumulator.hpp:128-138) */
+/* hit_accumulator::use (hit_accumulator.hpp:128-138); fixed: the flux as an
+ * int64 multiple of 2^-32, rounded to nearest even like the GPU */
 static inline void acc_use(acc_t* a, int32_t p, float v) {
   double dv = (double)v;
-  a->s1[p] += dv;
+  if (a->fixed) {
+    int64_t q;
+    memcpy(&q, &a->s1[p], 8);
+    q += (int64_t)llrint(dv * 4294967296.0);
+    memcpy(&a->s1[p], &q, 8);
+  } else {
+    a->s1[p] += dv;
+  }
   a->s2[p] += dv * v;
   a->s3[p] += dv * v * v;
   a->s4[p] += dv * v * v * v;
@@ -1001,6 +1010,7 @@ int orc_trace(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, 
   {
     acc_t a;
     memset(&a, 0, sizeof a);
+    a.fixed = cf->accum_fixed != 0;
     a.s1 = (double*)calloc((size_t)np + 1, sizeof(double));
     a.s2 = (double*)calloc((size_t)np + 1, sizeof(double));
     a.s3 = (double*)calloc((size_t)np + 1, sizeof(double));
@@ -1011,7 +1021,16 @@ int orc_trace(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, 
 #pragma omp critical
     {
       for (int64_t p = 0; p < np; ++p) {
-        s1[p] += a.s1[p]; s2[p] += a.s2[p]; s3[p] += a.s3[p]; s4[p] += a.s4[p];
+        if (a.fixed) {  /* s1 of the caller holds the integer sums until the end */
+          int64_t x, y;
+          memcpy(&x, &s1[p], 8);
+          memcpy(&y, &a.s1[p], 8);
+          x += y;
+          memcpy(&s1[p], &x, 8);
+        } else {
+          s1[p] += a.s1[p];
+        }
+        s2[p] += a.s2[p]; s3[p] += a.s3[p]; s4[p] += a.s4[p];
         cnt[p] += a.cnt[p];
       }
       tally->hitc += a.t.hitc;
@@ -1023,6 +1042,12 @@ int orc_trace(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, 
     }
     free(a.s1); free(a.s2); free(a.s3); free(a.s4); free(a.cnt);
   }
+  if (cf->accum_fixed)
+    for (int64_t p = 0; p < np; ++p) {
+      int64_t x;
+      memcpy(&x, &s1[p], 8);
+      s1[p] = (double)x * (1.0 / 4294967296.0);
+    }
   return 0;
 }
 

@@ -44,6 +44,7 @@ typedef struct orc_config {
   const float* sticking_field; /* per-primitive sticking, or NULL */
   int32_t  window;             /* 1: multi-hit window deposit (point_cloud_context.hpp) */
   float    window_factor;      /* window length in radii of the disc that opens it (rti: 5) */
+  int32_t  accum_fixed;        /* 1: S1 summed as int64 multiples of 2^-32 (order-independent) */
 } orc_config;
 
 typedef struct orc_tally {

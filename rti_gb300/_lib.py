@@ -44,7 +44,7 @@ EXPORTS = [
     "rtg_get_tree_depth", "rtg_autotune", "rtg_batch_set_launch_config", "rtg_batch_get_launch_config",
     "rtg_batch_autotune", "rtg_write_vtp", "rtg_write_vtp_discs", "rtg_write_vtp_triangles", "rtg_write_vtp_mixed",
     "rtg_read_point_cloud", "rtg_read_triangles", "rtg_set_tree_builder", "rtg_get_tree_builder",
-    "rtg_set_deposit_mode", "rtg_get_deposit_mode",
+    "rtg_set_deposit_mode", "rtg_get_deposit_mode", "rtg_set_accumulation", "rtg_get_accumulation",
 ]
 
 RTG_ADJ_HELD = 0
@@ -59,6 +59,8 @@ RTG_TREE_PLOC = 1
 RTG_STACK_AUTO = 0
 RTG_STACK_LOCAL = 1
 RTG_STACK_SHARED = 2
+RTG_ACCUM_FP64 = 0
+RTG_ACCUM_FIXED = 1
 RTG_DEPOSIT_NEIGHBORS = 0
 RTG_DEPOSIT_WINDOW = 1
 
@@ -198,6 +200,8 @@ def load(path: str | None = None):
         "rtg_get_tree_builder": (C.c_int, [_ctx, _i32p]),
         "rtg_set_deposit_mode": (C.c_int, [_ctx, C.c_int32, C.c_float]),
         "rtg_get_deposit_mode": (C.c_int, [_ctx, _i32p, _f32p]),
+        "rtg_set_accumulation": (C.c_int, [_ctx, C.c_int32]),
+        "rtg_get_accumulation": (C.c_int, [_ctx, _i32p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -405,6 +405,7 @@ int prepare_trace_with(rtg_context* ctx, const rtg_config& c, const float* box_l
   p.max_segments = c.max_segments;
   p.job = c.job;
   p.adj_inv_n1 = 1.0 / ((double)c.source_exponent + 1.0);
+  p.fixed_s1 = ctx->accum == RTG_ACCUM_FIXED ? 1 : 0;
   p.window = ctx->deposit_mode == RTG_DEPOSIT_WINDOW ? 1 : 0;
   p.window_factor = ctx->window_factor;
   return RTG_OK;
@@ -727,6 +728,20 @@ int rtg_set_deposit_mode(rtg_context* ctx, int32_t mode, float window_factor) {
   return RTG_OK;
 }
 
+int rtg_set_accumulation(rtg_context* ctx, int32_t mode) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (mode != RTG_ACCUM_FP64 && mode != RTG_ACCUM_FIXED)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "mode must be RTG_ACCUM_FP64 or RTG_ACCUM_FIXED");
+  ctx->accum = mode;
+  return RTG_OK;
+}
+
+int rtg_get_accumulation(const rtg_context* ctx, int32_t* mode) {
+  if (!ctx || !mode) return RTG_ERR_INVALID_ARGUMENT;
+  *mode = ctx->accum;
+  return RTG_OK;
+}
+
 int rtg_get_deposit_mode(const rtg_context* ctx, int32_t* mode, float* window_factor) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   if (mode) *mode = ctx->deposit_mode;
@@ -841,9 +856,12 @@ int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint
   } else {
     RTG_CUDA(ctx, cudaMemsetAsync(&ctx->d_tally->next_ray, 0, sizeof(unsigned long long), st));
   }
+  const bool fixed = p.fixed_s1 != 0;
+  if (fixed && accumulate) RTG_TRY(s1_to_fixed(ctx, ctx->acc.p, np, st));  // resume the integer sums
   RTG_CUDA(ctx, cudaEventRecord(ctx->evk0, st));
   if (ray_end > ray_begin) RTG_TRY(launch_trace(ctx, p, st));
   RTG_CUDA(ctx, cudaEventRecord(ctx->evk1, st));
+  if (fixed) RTG_TRY(s1_to_double(ctx, ctx->acc.p, np, st));
   RTG_TRY(compute_areas(ctx, st, ctx->box_lo, ctx->box_hi));
   RTG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   ctx->last_rays += ray_end - ray_begin;

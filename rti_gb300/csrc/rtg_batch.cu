@@ -159,6 +159,8 @@ int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint6
     return set_error(ctx, RTG_ERR_NO_GEOMETRY, "scene has no geometry");
   if (scene->deposit_mode != RTG_DEPOSIT_NEIGHBORS)
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a batch traces the neighbour deposit only");
+  if (scene->accum != RTG_ACCUM_FP64)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a batch accumulates in FP64 only");
   if (b->jobs.size() >= 0x7FFFFFFF) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "too many jobs");
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));
   Job j;

@@ -79,6 +79,7 @@ struct TraceParams {
   uint32_t job;
   int32_t packet;  // a warp takes new source rays when at least this many lanes are idle
   int32_t plain;   // 1: one source ray per thread, no refill (grid covers all rays)
+  int32_t fixed_s1;       // 1: s1 holds int64 multiples of 2^-32 during the trace (RTG_ACCUM_FIXED)
   int32_t window;         // 1: multi-hit window deposit (RTG_DEPOSIT_WINDOW), traced by kModeWindow
   float window_factor;    // window length in radii of the disc that opens it
   // adjoint replay (unused by the forward trace)
@@ -173,6 +174,7 @@ struct rtg_context {
   float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
   rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL, RTG_LEAF_IMMEDIATE};
   int32_t deposit_mode = RTG_DEPOSIT_NEIGHBORS;
+  int32_t accum = RTG_ACCUM_FP64;
   float window_factor = 5.0f;  // point_cloud_context.hpp:163
   rtg::Wavefront wf;
   std::string err;
@@ -200,6 +202,9 @@ int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float t
 SceneView scene_view(rtg_context* ctx);
 // stack entries for a requested depth (0 = automatic) and a tree depth: 32, 64 or 256
 int stack_for(int requested, int tree_depth);
+// RTG_ACCUM_FIXED: s1 between double and int64 multiples of 2^-32, in place
+int s1_to_fixed(rtg_context* ctx, double* s1, int64_t n, cudaStream_t st);
+int s1_to_double(rtg_context* ctx, double* s1, int64_t n, cudaStream_t st);
 // whether a trace of ctx under lc keeps its traversal stacks in shared memory
 bool shared_stack(rtg_context* ctx, const rtg_launch_config& lc);
 int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc);

@@ -218,10 +218,14 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   return bid != INT_MAX;
 }
 
-// hit_accumulator::use (hit_accumulator.hpp:128-138)
+// hit_accumulator::use (hit_accumulator.hpp:128-138); with fixed_s1 the flux
+// is added as an int64 multiple of 2^-32 (order-independent sums)
 __device__ __forceinline__ void deposit(const TraceParams& p, int id, float v) {
   const double dv = (double)v;
-  atomicAdd(&p.s1[id], dv);
+  if (p.fixed_s1)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&p.s1[id]), (unsigned long long)__double2ll_rn(dv * 4294967296.0));
+  else
+    atomicAdd(&p.s1[id], dv);
   atomicAdd(&p.s2[id], dv * v);
   atomicAdd(&p.s3[id], dv * v * v);
   atomicAdd(&p.s4[id], dv * v * v * v);

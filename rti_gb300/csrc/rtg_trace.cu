@@ -64,6 +64,34 @@ PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, bool shared,
 
 }  // namespace
 
+namespace {
+
+__global__ void s1_fixed_kernel(double* s1, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) reinterpret_cast<long long*>(s1)[i] = __double2ll_rn(s1[i] * 4294967296.0);
+}
+
+__global__ void s1_double_kernel(double* s1, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) s1[i] = (double)reinterpret_cast<const long long*>(s1)[i] * (1.0 / 4294967296.0);
+}
+
+}  // namespace
+
+int s1_to_fixed(rtg_context* ctx, double* s1, int64_t n, cudaStream_t st) {
+  if (n <= 0) return RTG_OK;
+  s1_fixed_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s1, n);
+  RTG_CUDA(ctx, cudaGetLastError());
+  return RTG_OK;
+}
+
+int s1_to_double(rtg_context* ctx, double* s1, int64_t n, cudaStream_t st) {
+  if (n <= 0) return RTG_OK;
+  s1_double_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s1, n);
+  RTG_CUDA(ctx, cudaGetLastError());
+  return RTG_OK;
+}
+
 bool shared_stack(rtg_context* ctx, const rtg_launch_config& lc) {
   if (lc.stack_memory == RTG_STACK_SHARED) return true;
   if (lc.stack_memory == RTG_STACK_LOCAL) return false;

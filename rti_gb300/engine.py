@@ -193,6 +193,16 @@ class Engine:
         self._check(self._L.rtg_get_deposit_mode(self._h, C.byref(m), C.byref(f)))
         return m.value, f.value
 
+    @property
+    def accumulation(self) -> int:
+        """L.RTG_ACCUM_FP64 or L.RTG_ACCUM_FIXED (order-independent, bit-reproducible S1)."""
+        m = C.c_int32()
+        self._check(self._L.rtg_get_accumulation(self._h, C.byref(m)))
+        return m.value
+
+    def set_accumulation(self, mode: int):
+        self._check(self._L.rtg_set_accumulation(self._h, int(mode)))
+
     def set_deposit_mode(self, mode: int, window_factor: float = 5.0):
         """Selects the deposit of a front-face disc hit for later traces."""
         self._check(self._L.rtg_set_deposit_mode(self._h, int(mode), float(window_factor)))

@@ -292,3 +292,38 @@ def test_independent_streams_agree_within_4_sigma(eng, trench, oracle_lib):
     ok = xg + xc > 0
     assert np.all(np.abs(xg - xc)[ok] <= 4 * np.sqrt(var[ok]))
     assert not np.array_equal(g["counts"], c.counts)  # the streams really are independent
+
+
+def test_fixed_point_flux_is_bit_exact(eng, trench, hole, oracle_lib):
+    """RTG_ACCUM_FIXED: the GPU's S1 equals the oracle's bit for bit (order-
+    independent integer sums), repeated traces give identical S1, and a trace
+    split into two accumulated ray ranges equals the whole trace."""
+    from rti_gb300 import RtgError, _lib as L
+    from rti_gb300.batch import Batch
+    eng.set_accumulation(L.RTG_ACCUM_FIXED)
+    assert eng.accumulation == L.RTG_ACCUM_FIXED
+    try:
+        _upload_discs(eng, trench, sticking=0.1, x_bound=1, y_bound=1)
+        n = 200000
+        g1 = _gpu_trace(eng, n, seed=11)
+        g2 = _gpu_trace(eng, n, seed=11)
+        s = oracle_lib.Scene(trench.xyzr, trench.normals)
+        s.neighbors()
+        c = s.trace(oracle_lib.make_config(trench.box_lo, trench.box_hi, sticking=0.1, seed=11, accum_fixed=1), 0, n)
+        assert np.array_equal(g1["s"][0], c.s1) and np.array_equal(g1["s"][0], g2["s"][0])
+        eng.trace(n // 2, 11)
+        eng.trace(n - n // 2, 11, ray_begin=n // 2, accumulate=True)
+        assert np.array_equal(eng.accumulators()[0], g1["s"][0])
+        eng.upload_triangles(hole.vertices, hole.indices)
+        eng.configure(box=(hole.box_lo, hole.box_hi), sticking=0.01, reflection=2, specular_fraction=0.1,
+                      x_bound=1, y_bound=1, reset=True)
+        g = _gpu_trace(eng, 100000, seed=3)
+        ch = oracle_lib.Scene(tri_vertices=hole.vertices, tri_indices=hole.indices).trace(
+            oracle_lib.make_config(hole.box_lo, hole.box_hi, sticking=0.01, reflection=2, specular_fraction=0.1,
+                                   seed=3, accum_fixed=1), 0, 100000)
+        assert np.array_equal(g["s"][0], ch.s1)
+        with Batch(0) as b:
+            with pytest.raises(RtgError, match="FP64"):
+                b.add(eng, 1000)
+    finally:
+        eng.set_accumulation(L.RTG_ACCUM_FP64)

@@ -42,3 +42,18 @@ def test_field_gradient_vs_crn_differences(oracle_lib, level):
         if not abs(fg[j] - fd) <= 1e-3 * max(abs(fd), 1e-6 * np.abs(fg).max()):
             bad += 1
     assert bad <= 1
+
+
+def test_oracle_fixed_point_flux_is_order_independent(oracle_lib):
+    """accum_fixed: S1 summed as integer multiples of 2^-32 does not depend on
+    how the rays are split over threads, and stays within 1e-6 of FP64 sums."""
+    from rti_gb300 import scenes
+    t = scenes.trench_discs(domain=1.2, width=0.4, depth=1.0)
+    s = oracle_lib.Scene(t.xyzr, t.normals)
+    s.neighbors()
+    cfg = lambda fixed: oracle_lib.make_config(t.box_lo, t.box_hi, sticking=0.1, seed=3, accum_fixed=fixed)
+    a = s.trace(cfg(1), 0, 40000, nthreads=1)
+    b = s.trace(cfg(1), 0, 40000, nthreads=4)
+    c = s.trace(cfg(0), 0, 40000, nthreads=4)
+    assert np.array_equal(a.s1, b.s1) and np.array_equal(a.counts, c.counts)
+    np.testing.assert_allclose(a.s1, c.s1, rtol=1e-6, atol=1e-9)
