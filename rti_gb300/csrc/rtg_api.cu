@@ -523,6 +523,7 @@ const char* rtg_last_error(const rtg_context* ctx) { return ctx ? ctx->err.c_str
 int rtg_upload_mixed(rtg_context* ctx, const float* points, const float* normals, const float* radii, int64_t nd,
                      const float* vertices, const uint32_t* indices, int64_t nv, int64_t nt) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  NvtxRange range("rtg upload + LBVH build");
   RTG_TRY(use_device(ctx));
   // both halves are checked before either replaces the context's surface
   Staged sg;
@@ -843,6 +844,7 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
 int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, int accumulate,
                     void* stream) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  NvtxRange range("rtg trace (enqueue)");
   TraceParams p{};
   RTG_TRY(prepare_trace(ctx, ray_begin, ray_end, seed, p));
   const int64_t np = ctx->g.nd + ctx->g.nt;
@@ -888,6 +890,7 @@ int rtg_set_sticking_field_device(rtg_context* ctx, const float* d_field, int64_
 int rtg_adjoint(rtg_context* ctx, const double* d_g, uint64_t ray_begin, uint64_t ray_end, uint64_t seed, int estimator,
                 double* d_field_grad, double* d_scalars, void* stream) {
   if (!ctx || !d_g || !d_scalars) return RTG_ERR_INVALID_ARGUMENT;
+  NvtxRange range("rtg adjoint (enqueue)");
   const bool field = ctx->sticking_field.p != nullptr;
   if (field && !d_field_grad)
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a sticking field is set: d_field_grad is required");

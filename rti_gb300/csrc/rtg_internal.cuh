@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "rtg.h"
 
 namespace rtg {
@@ -181,6 +183,15 @@ struct rtg_context {
 };
 
 namespace rtg {
+
+// A named range on the host timeline for profilers (NVTX; a no-op unless a
+// profiling tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // sort.cu
 int exclusive_scan_u32(rtg_context* ctx, uint32_t* d_a, int64_t m, uint32_t* d_total, cudaStream_t st);
