@@ -19,6 +19,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librtg.so")
+LIB_CHECKED = os.path.join(HERE, "librtg_checked.so")  # -DRTG_CHECKED: device bounds checks (tests)
 SOURCES = ["rtg_api.cu", "rtg_batch.cu", "rtg_lbvh.cu", "rtg_noalloc.cu", "rtg_sort.cu", "rtg_surface.cu", "rtg_trace.cu",
            "rtg_trace_batched.cu", "rtg_vtk.cpp", "rtg_wavefront.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -58,24 +59,31 @@ def _deps() -> list[str]:
     return files
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None, checked: bool = False) -> str:
+    """librtg.so; checked=True: librtg_checked.so, the same with -DRTG_CHECKED
+    (every index read from device data verified before use, a bad one counted
+    in the trace's errors), for tests."""
+    lib = LIB_CHECKED if checked else LIB
+    if not force and up_to_date(lib):
+        return lib
+    bdir = BUILD + ("_checked" if checked else "")
+    os.makedirs(bdir, exist_ok=True)
     exe = nvcc()
     extra = list(extra or [])
     zdef, zlink = zlib_flags()
     extra += zdef
+    if checked:
+        extra.append("-DRTG_CHECKED")
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+        obj = os.path.join(bdir, os.path.splitext(src)[0] + ".o")
         cmd = [exe, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -86,14 +94,15 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
 
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, *zlink, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    build_cli()
-    return LIB
+    os.replace(tmp, lib)
+    if not checked:
+        build_cli()
+    return lib
 
 
 def build_cli() -> str:

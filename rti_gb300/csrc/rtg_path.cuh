@@ -30,6 +30,22 @@ namespace rtg {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// A build with -DRTG_CHECKED verifies every node, slot, primitive and
+// neighbour index read from device data before it is used, and counts a bad
+// one as an error (tally.errors) instead of dereferencing it.
+#ifdef RTG_CHECKED
+constexpr bool kChecked = true;
+#else
+constexpr bool kChecked = false;
+#endif
+
+__device__ __forceinline__ bool node_in_range(const SceneView& s, uint32_t cur) {
+  return cur < (s.nd + s.nt > 1 ? (uint32_t)(s.nd + s.nt - 1) : 1u);
+}
+__device__ __forceinline__ bool leaf_in_range(const SceneView& s, uint32_t ref) {
+  return (ref & kTriBit) ? (ref & kSlotMask) < (uint32_t)s.nt : (ref & kSlotMask) < (uint32_t)s.nd;
+}
 constexpr uint32_t kNoLeaf = 0xFFFFFFFFu;  // no child reference: slots stay below kSlotMask
 
 __device__ __forceinline__ float safe_inv(float d) {
@@ -124,6 +140,10 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
         errs += 1;
         break;
       }
+      if (kChecked && !node_in_range(s, cur)) {
+        errs += 1;
+        break;
+      }
       float4 a, b, c;
       uint4 ch;
       load_node(s.nodes + cur, a, b, c, ch);
@@ -137,7 +157,8 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
       uint32_t lf = l0 ? ch.x : (l1 ? ch.y : kNoLeaf);
       uint32_t lf2 = l0 && l1 ? ch.y : kNoLeaf;
       while (lf != kNoLeaf) {
-        test_leaf(s, lf, r, tnear, bt, bid, bref);
+        if (!kChecked || leaf_in_range(s, lf)) test_leaf(s, lf, r, tnear, bt, bid, bref);
+        else errs += 1;
         lf = lf2;
         lf2 = kNoLeaf;
       }
@@ -176,6 +197,11 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
         cur = kNone;
         break;
       }
+      if (kChecked && !node_in_range(s, cur)) {
+        errs += 1;
+        cur = kNone;
+        break;
+      }
       float4 a, b, c;
       uint4 ch;
       load_node(s.nodes + cur, a, b, c, ch);
@@ -207,7 +233,8 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
         cur = kNone;
         break;
       }
-      test_leaf(s, leaf, r, tnear, bt, bid, bref);
+      if (!kChecked || leaf_in_range(s, leaf)) test_leaf(s, leaf, r, tnear, bt, bid, bref);
+      else errs += 1;
       leaf = kNone;
       if (cur != kNone && (cur & kLeafBit)) {
         leaf = cur;
@@ -255,6 +282,10 @@ __device__ void leaves_in_interval(const SceneView& s, const Ray& r, float tlo, 
   const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
   for (int64_t it = 0;; ++it) {
     if (it > max_iter) {
+      errs += 1;
+      return;
+    }
+    if (kChecked && !node_in_range(s, cur)) {
       errs += 1;
       return;
     }
@@ -308,6 +339,10 @@ __device__ float window_deposit(const TraceParams& p, f3 o, f3 d, float t0, floa
   if (tbox < te) te = tbox;
   // hit of the leaf primitive in slot lr: t, id, and whether it closes the window
   auto leaf = [&](uint32_t lr, float& t, int& id, bool& closes) -> bool {
+    if (kChecked && !leaf_in_range(p.s, lr)) {
+      errs += 1;
+      return false;
+    }
     const uint32_t slot = lr & kSlotMask;
     if (lr & kTriBit) {
       const float4 a = __ldg(&p.s.tri[4 * (int64_t)slot]), b = __ldg(&p.s.tri[4 * (int64_t)slot + 1]);
@@ -551,6 +586,11 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
     uint32_t href;
     const bool hit = closest_hit<STACK, POSTPONE, kSst>(pp->s, o, d, pp->tnear, th, hid, href, c_err, sstk);
     const int axis = boundary_exit(*pp, o, d, tb);
+    if (kChecked && hit && (unsigned)hid >= (unsigned)(pp->s.nd + pp->s.nt)) {
+      c_err += 1;
+      active = path_end();
+      continue;
+    }
     if (hit && (axis < 0 || th <= tb)) {
       float4 nn;
       if (href & kTriBit) nn = __ldg(&pp->s.tri[4 * (int64_t)(href & kSlotMask) + 3]);
@@ -576,11 +616,20 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
       if (M != kModeWindow && !(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
         const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
         for (int64_t q = q0; q < q1; ++q) {
+          const uint32_t ns = __ldg(&pp->s.nb_slot[q]);
+          if (kChecked && ns >= (uint32_t)pp->s.nd) {
+            c_err += 1;
+            continue;
+          }
           float4 cr, nv;  // the neighbour's slot record: (centre, radius), (normal, id bits)
           asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
               : "=f"(cr.x), "=f"(cr.y), "=f"(cr.z), "=f"(cr.w), "=f"(nv.x), "=f"(nv.y), "=f"(nv.z), "=f"(nv.w)
-              : "l"(pp->s.disc + 2 * (int64_t)__ldg(&pp->s.nb_slot[q])));
+              : "l"(pp->s.disc + 2 * (int64_t)ns));
           const int nb = __float_as_int(nv.w);
+          if (kChecked && (unsigned)nb >= (unsigned)pp->s.nd) {
+            c_err += 1;
+            continue;
+          }
           if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
             if (kAdj) G += __ldg(&pp->adj_g[nb]);
             else deposit(*pp, nb, v);

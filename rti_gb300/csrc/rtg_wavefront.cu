@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(TPB) wf_shade_kernel(const TraceParams* __rest
   const unsigned lt_mask = (1u << lane) - 1u;
   const int nxt = cur ^ 1;
   const uint64_t n = b.ctl[kCtlCur] + b.ctl[kCtlGenCount];
-  unsigned long long c_hit = 0, c_non = 0, c_tot = 0, c_trunc = 0, c_nb = 0;
+  unsigned long long c_hit = 0, c_non = 0, c_tot = 0, c_trunc = 0, c_nb = 0, c_err = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * TPB + threadIdx.x; i < n; i += (uint64_t)gridDim.x * TPB) {
     const float4 a = b.ow[cur][i], c = b.dk[cur][i];
     const uint4 m = b.meta[cur][i];
@@ -141,7 +141,9 @@ __global__ void __launch_bounds__(TPB) wf_shade_kernel(const TraceParams* __rest
     bool cont = false;
     float tb = 0.0f;
     const int axis = boundary_exit(*pp, o, d, tb);
-    if (hid >= 0 && (axis < 0 || th <= tb)) {
+    if (kChecked && hid >= pp->s.nd + pp->s.nt) {  // a bad hit id ends the path, counted
+      c_err += 1;
+    } else if (hid >= 0 && (axis < 0 || th <= tb)) {
       float4 nn;
       if (href & kTriBit) nn = __ldg(&pp->s.tri[4 * (int64_t)(href & kSlotMask) + 3]);
       else nn = __ldg(&pp->s.disc[2 * (int64_t)(href & kSlotMask) + 1]);
@@ -159,12 +161,21 @@ __global__ void __launch_bounds__(TPB) wf_shade_kernel(const TraceParams* __rest
         if (!(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
           const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
           for (int64_t q = q0; q < q1; ++q) {
+            const uint32_t ns = __ldg(&pp->s.nb_slot[q]);
+            if (kChecked && ns >= (uint32_t)pp->s.nd) {
+              c_err += 1;
+              continue;
+            }
             float4 cr, nb_n;  // the neighbour's slot record
             asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                 : "=f"(cr.x), "=f"(cr.y), "=f"(cr.z), "=f"(cr.w), "=f"(nb_n.x), "=f"(nb_n.y), "=f"(nb_n.z),
                   "=f"(nb_n.w)
-                : "l"(pp->s.disc + 2 * (int64_t)__ldg(&pp->s.nb_slot[q])));
+                : "l"(pp->s.disc + 2 * (int64_t)ns));
             const int nb = __float_as_int(nb_n.w);
+            if (kChecked && (unsigned)nb >= (unsigned)pp->s.nd) {
+              c_err += 1;
+              continue;
+            }
             if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nb_n.x, nb_n.y, nb_n.z))) {
               deposit(*pp, nb, v);
               c_tot += 1;
@@ -231,7 +242,7 @@ __global__ void __launch_bounds__(TPB) wf_shade_kernel(const TraceParams* __rest
       b.meta[nxt][slot] = make_uint4(m.x, m.y, m.z, nseg);
     }
   }
-  flush_counts(tally, c_hit, c_non, c_tot, 0, c_trunc, c_nb, 0);
+  flush_counts(tally, c_hit, c_non, c_tot, 0, c_trunc, c_nb, c_err);
   // the last block to finish schedules the next wave
   __syncthreads();
   if (threadIdx.x == 0) {
