@@ -154,7 +154,11 @@ RTG_API const char* rtg_last_error(const rtg_context* ctx);
  * the neighbour lists.  Replaces any previous geometry; clears the sticking
  * field.  The arrays are checked on the device before anything is replaced:
  * a refused upload (non-finite value, radius <= 0, normal not of unit length,
- * index out of range) leaves the previous surface as it was. */
+ * index out of range) leaves the previous surface as it was.  An upload,
+ * update (rtg_update_*) or tree rebuild (rtg_set_tree_builder) that fails
+ * after that point -- RTG_ERR_OUT_OF_MEMORY while the tree is built, a CUDA
+ * error -- leaves the context without a surface: traces report
+ * RTG_ERR_NO_GEOMETRY until an upload succeeds. */
 RTG_API int rtg_upload_discs(rtg_context* ctx, const float* points, const float* normals, const float* radii,
                      int64_t n);
 /* vertices: nv x 3, indices: nt x 3 (uint32).  Replaces any previous geometry. */
@@ -229,6 +233,20 @@ RTG_API int rtg_get_deposit_mode(const rtg_context* ctx, int32_t* mode, float* w
 #define RTG_ACCUM_FIXED 1
 RTG_API int rtg_set_accumulation(rtg_context* ctx, int32_t mode);
 RTG_API int rtg_get_accumulation(const rtg_context* ctx, int32_t* mode);
+/* Work limit of one closest-hit query: after `visits` tree nodes the query
+ * ends and counts as an error (tally.errors), the getters of that trace then
+ * return RTG_ERR_BUDGET.  0 (default) = 4 x primitives + 64, which a valid
+ * tree never reaches; a larger value is capped there.  Bounds the work of a
+ * trace on a damaged or adversarial tree.  Applies to later traces. */
+RTG_API int rtg_set_visit_limit(rtg_context* ctx, uint64_t visits);
+RTG_API int rtg_get_visit_limit(const rtg_context* ctx, uint64_t* visits);
+/* Fault injection for tests of the error paths: after `after` further device
+ * allocations of this context succeed, the next one fails as if the device
+ * were out of memory (once); after < 0 cancels.  The call that meets it
+ * returns RTG_ERR_OUT_OF_MEMORY; an upload, update or rebuild then leaves the
+ * context without a surface (see rtg_upload_discs), any other call leaves the
+ * context as it was. */
+RTG_API int rtg_inject_alloc_failure(rtg_context* ctx, int64_t after);
 /* Autotuner: for each tree builder (RTG_TREE_*), times each candidate launch
  * configuration (block size x packet x stack depth x scheduling) on source
  * rays [0, sample_rays) with `seed` under the current surface and
@@ -275,7 +293,9 @@ RTG_API int rtg_adjoint_host(rtg_context* ctx, const double* g, uint64_t n_rays,
                              double* field_grad, double* d_sticking, double* d_exponent);
 
 /* Closest hit for explicit rays: rays = n x 6 floats (origin, direction),
- * host pointers.  prim_out = primitive id or -1, t_out = distance. */
+ * host pointers.  prim_out = primitive id or -1, t_out = distance.
+ * Synchronous; RTG_ERR_BUDGET when a query reached the visit limit (its
+ * result is then the closest hit found before it stopped). */
 RTG_API int rtg_trace_rays(rtg_context* ctx, const float* rays, int64_t n, float tnear, int32_t* prim_out,
                    float* t_out);
 
@@ -365,10 +385,12 @@ RTG_API int rtg_get_device_view(rtg_context* ctx, rtg_device_view* view);
  * (use_graph != 0: the zeroing, the launch and the area kernels are captured
  * into a CUDA graph on the first run and replayed afterwards);
  * rtg_batch_run_sequential issues one plain launch per job, with the same
- * results.  A job keeps the device addresses of its context's geometry as of
- * rtg_batch_add: re-uploading a context's geometry (rtg_upload_*) needs a new
- * batch; refits (rtg_update_*) and new values of a sticking field that was
- * already set (same size) at rtg_batch_add are seen by later runs.
+ * results.  A job keeps its configuration, ray count and seed from
+ * rtg_batch_add and reads its context's surface when the batch runs: refits
+ * (rtg_update_*), a new tree, a sticking field set or cleared, a new visit
+ * limit and a new upload of as many primitives are seen by later runs; a run
+ * whose job's context now holds another number of primitives (or none), or is
+ * in window deposit or fixed-point mode, fails with RTG_ERR_INVALID_ARGUMENT.
  * The contexts must outlive the batch and must not trace while it runs. */
 typedef struct rtg_batch rtg_batch;
 RTG_API int rtg_batch_create(rtg_batch** out, int device);
@@ -382,7 +404,8 @@ RTG_API int rtg_batch_run(rtg_batch* b, int use_graph, void* stream);
 RTG_API int rtg_batch_run_sequential(rtg_batch* b, void* stream);
 /* Waits for the last run; *elapsed_ms = its device time (may be NULL). */
 RTG_API int rtg_batch_synchronize(rtg_batch* b, double* elapsed_ms);
-/* Job results (host buffers of the job's primitive count; any may be NULL):
+/* Job results (host buffers of the job's primitive count, its context's at
+ * rtg_batch_add; any may be NULL):
  * S1 (hit_accumulator.hpp:140-142), hit counts (:144-146), exposed areas. */
 RTG_API int rtg_batch_get_results(rtg_batch* b, int32_t job, double* s1, uint64_t* counts, float* areas);
 /* Counters over all jobs of the last run. */

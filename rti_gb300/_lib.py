@@ -45,6 +45,7 @@ EXPORTS = [
     "rtg_batch_autotune", "rtg_write_vtp", "rtg_write_vtp_discs", "rtg_write_vtp_triangles", "rtg_write_vtp_mixed",
     "rtg_read_point_cloud", "rtg_read_triangles", "rtg_set_tree_builder", "rtg_get_tree_builder",
     "rtg_set_deposit_mode", "rtg_get_deposit_mode", "rtg_set_accumulation", "rtg_get_accumulation",
+    "rtg_set_visit_limit", "rtg_get_visit_limit", "rtg_inject_alloc_failure",
 ]
 
 RTG_ADJ_HELD = 0
@@ -200,6 +201,9 @@ def load(path: str | None = None):
         "rtg_get_tree_builder": (C.c_int, [_ctx, _i32p]),
         "rtg_set_deposit_mode": (C.c_int, [_ctx, C.c_int32, C.c_float]),
         "rtg_get_deposit_mode": (C.c_int, [_ctx, _i32p, _f32p]),
+        "rtg_set_visit_limit": (C.c_int, [_ctx, C.c_uint64]),
+        "rtg_get_visit_limit": (C.c_int, [_ctx, _u64p]),
+        "rtg_inject_alloc_failure": (C.c_int, [_ctx, C.c_int64]),
         "rtg_set_accumulation": (C.c_int, [_ctx, C.c_int32]),
         "rtg_get_accumulation": (C.c_int, [_ctx, _i32p]),
     }

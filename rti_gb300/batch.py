@@ -27,12 +27,14 @@ class Batch:
         if rc != L.RTG_OK:
             raise L.RtgError(rc, "rtg_batch_create failed (no usable CUDA device?)")
         self._scenes: list[Engine] = []  # keeps the contexts alive as long as the batch
+        self._sizes: list[int] = []
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             self._L.rtg_batch_destroy(self._h)
             self._h = C.c_void_p()
         self._scenes = []
+        self._sizes = []
 
     def __del__(self):
         try:
@@ -57,6 +59,7 @@ class Batch:
         self._check(self._L.rtg_batch_add(self._h, scene._h, None if config is None else C.byref(config),
                                           int(n_rays), int(seed), C.byref(j)))
         self._scenes.append(scene)
+        self._sizes.append(scene.num_primitives)  # the job's accumulators have this size
         return j.value
 
     def __len__(self) -> int:
@@ -86,7 +89,7 @@ class Batch:
 
     def results(self, job: int):
         """(S1, hit counts, exposed areas) of one job."""
-        n = self._scenes[job].num_primitives
+        n = self._sizes[job]
         s1 = np.zeros(n)
         cnt = np.zeros(n, dtype=np.uint64)
         areas = np.zeros(n, dtype=np.float32)

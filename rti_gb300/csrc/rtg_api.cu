@@ -359,6 +359,23 @@ int commit(rtg_context* ctx, const Staged& sg) {
 
 }  // namespace
 
+void drop_surface(rtg_context* ctx) {
+  cudaStreamSynchronize(ctx->stream);
+  Geometry& g = ctx->g;
+  dfree(g.disc_cr_by_id); dfree(g.disc_n_by_id); dfree(g.tri_v); dfree(g.tri_idx);
+  dfree(g.disc); dfree(g.tri); dfree(g.nodes);
+  dfree(g.leaf_ref); dfree(g.leaf_prim); dfree(g.parent); dfree(g.prim_lo); dfree(g.prim_hi);
+  dfree(g.refit_flags); dfree(g.nb_ptr); dfree(g.nb_idx); dfree(g.nb_slot); dfree(g.disc_slot);
+  dfree(ctx->sticking_field);
+  g.nd = g.nt = g.nv = 0;
+  g.nb_nnz = 0;
+  g.root = 0;
+  g.depth = 0;
+  ctx->traced = false;
+  ctx->finalized = false;
+  ++ctx->version;
+}
+
 // Checks the context and fills the kernel parameters of a trace (or of its
 // adjoint replay) of source rays [ray_begin, ray_end) under configuration c
 // and trace box box_lo/box_hi; accumulators and counters are the context's.
@@ -530,11 +547,18 @@ int rtg_upload_mixed(rtg_context* ctx, const float* points, const float* normals
   int rc = stage_discs(ctx, points, normals, radii, nd, sg);
   if (rc == RTG_OK) rc = stage_triangles(ctx, vertices, indices, nv, nt, sg);
   if (rc == RTG_OK && nd + nt == 0) rc = set_error(ctx, RTG_ERR_NO_GEOMETRY, "no primitives");
-  if (rc == RTG_OK) rc = commit(ctx, sg);
+  const bool committing = rc == RTG_OK;
+  if (committing) {
+    ++ctx->version;
+    rc = commit(ctx, sg);
+  }
   release(sg, ctx->stream);
-  RTG_TRY(rc);
-  dfree(ctx->sticking_field);
-  return rebuild_all(ctx);
+  if (committing) {
+    dfree(ctx->sticking_field);
+    if (rc == RTG_OK) rc = rebuild_all(ctx);
+    if (rc != RTG_OK) drop_surface(ctx);
+  }
+  return rc;
 }
 
 int rtg_upload_discs(rtg_context* ctx, const float* points, const float* normals, const float* radii, int64_t n) {
@@ -553,12 +577,20 @@ int rtg_update_discs(rtg_context* ctx, const float* points, const float* normals
     return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "update_discs: the disc count must not change");
   Staged sg;
   int rc = stage_discs(ctx, points, normals, radii, n, sg);
-  if (rc == RTG_OK) rc = commit(ctx, sg);
+  const bool committing = rc == RTG_OK;
+  if (committing) {
+    ++ctx->version;
+    rc = commit(ctx, sg);
+  }
   release(sg, ctx->stream);
-  RTG_TRY(rc);
-  RTG_TRY(refit_lbvh(ctx));
-  RTG_TRY(build_neighbors(ctx));
-  RTG_TRY(alloc_results(ctx));
+  if (!committing) return rc;
+  if (rc == RTG_OK) rc = refit_lbvh(ctx);
+  if (rc == RTG_OK) rc = build_neighbors(ctx);
+  if (rc == RTG_OK) rc = alloc_results(ctx);
+  if (rc != RTG_OK) {
+    drop_surface(ctx);
+    return rc;
+  }
   resolve_box(ctx);
   return RTG_OK;
 }
@@ -583,9 +615,15 @@ int rtg_update_vertices(rtg_context* ctx, const float* vertices, int64_t nv) {
     g.tri_min[a] = lo[a];
     g.tri_max[a] = hi[a];
   }
-  RTG_CUDA(ctx, cudaMemcpyAsync(g.tri_v.p, v.data(), nv * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
-  RTG_TRY(refit_lbvh(ctx));
-  RTG_TRY(alloc_results(ctx));
+  ++ctx->version;
+  int rc = check_cuda(ctx, cudaMemcpyAsync(g.tri_v.p, v.data(), nv * sizeof(float4), cudaMemcpyHostToDevice,
+                                           ctx->stream), "vertex update");
+  if (rc == RTG_OK) rc = refit_lbvh(ctx);
+  if (rc == RTG_OK) rc = alloc_results(ctx);
+  if (rc != RTG_OK) {
+    drop_surface(ctx);
+    return rc;
+  }
   resolve_box(ctx);
   return RTG_OK;
 }
@@ -651,6 +689,7 @@ int rtg_set_sticking(rtg_context* ctx, float s) {
 int rtg_set_sticking_field(rtg_context* ctx, const float* s, int64_t n) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   RTG_TRY(use_device(ctx));
+  ++ctx->version;
   if (!s) {
     dfree(ctx->sticking_field);
     return RTG_OK;
@@ -703,9 +742,14 @@ int rtg_set_tree_builder(rtg_context* ctx, int32_t builder) {
   const int32_t keep = ctx->g.builder;
   ctx->g.builder = builder;
   if (ctx->g.nd + ctx->g.nt > 0 && ctx->g.nodes.p && builder != keep) {
-    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    RTG_TRY(build_lbvh(ctx));
-    RTG_TRY(build_neighbors(ctx));  // neighbour columns are stored as slots of the new tree
+    ++ctx->version;
+    int rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "tree rebuild");
+    if (rc == RTG_OK) rc = build_lbvh(ctx);
+    if (rc == RTG_OK) rc = build_neighbors(ctx);  // neighbour columns are stored as slots of the new tree
+    if (rc != RTG_OK) {
+      drop_surface(ctx);
+      return rc;
+    }
     ctx->traced = false;
     ctx->finalized = false;
   }
@@ -740,6 +784,25 @@ int rtg_set_accumulation(rtg_context* ctx, int32_t mode) {
 int rtg_get_accumulation(const rtg_context* ctx, int32_t* mode) {
   if (!ctx || !mode) return RTG_ERR_INVALID_ARGUMENT;
   *mode = ctx->accum;
+  return RTG_OK;
+}
+
+int rtg_set_visit_limit(rtg_context* ctx, uint64_t visits) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  ctx->visit_limit = visits;
+  ++ctx->version;
+  return RTG_OK;
+}
+
+int rtg_inject_alloc_failure(rtg_context* ctx, int64_t after) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  ctx->alloc_failure_in = after < 0 ? -1 : after;
+  return RTG_OK;
+}
+
+int rtg_get_visit_limit(const rtg_context* ctx, uint64_t* visits) {
+  if (!ctx || !visits) return RTG_ERR_INVALID_ARGUMENT;
+  *visits = ctx->visit_limit;
   return RTG_OK;
 }
 
@@ -849,6 +912,7 @@ int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint
   RTG_TRY(prepare_trace(ctx, ray_begin, ray_end, seed, p));
   const int64_t np = ctx->g.nd + ctx->g.nt;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->traced = false;  // until this trace is enqueued in full
   RTG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   if (!accumulate) {
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * np * sizeof(double), st));
@@ -875,6 +939,7 @@ int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint
 int rtg_set_sticking_field_device(rtg_context* ctx, const float* d_field, int64_t n, void* stream) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   RTG_TRY(use_device(ctx));
+  ++ctx->version;
   if (!d_field) {
     dfree(ctx->sticking_field);
     return RTG_OK;
@@ -979,18 +1044,22 @@ int rtg_trace_rays(rtg_context* ctx, const float* rays, int64_t n, float tnear, 
   RTG_TRY(use_device(ctx));
   DBuf<float> dr, dt;
   DBuf<int32_t> dp;
+  DBuf<unsigned long long> de;  // queries that hit a traversal limit (the trace tally stays untouched)
   int rc = dalloc(ctx, dr, (size_t)(6 * n), "rays");
   if (rc == RTG_OK) rc = dalloc(ctx, dt, (size_t)n, "ray t");
   if (rc == RTG_OK) rc = dalloc(ctx, dp, (size_t)n, "ray prim");
+  if (rc == RTG_OK) rc = dalloc(ctx, de, 1, "ray errors");
+  unsigned long long errors = 0;
   if (rc == RTG_OK) {
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaMemcpyAsync(dr.p, rays, 6 * n * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(&ctx->d_tally->errors, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(de.p, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) rc = check_cuda(ctx, e, "trace_rays upload");
-    if (rc == RTG_OK) rc = launch_closest_hit(ctx, dr.p, n, tnear, dp.p, dt.p, st);
+    if (rc == RTG_OK) rc = launch_closest_hit(ctx, dr.p, n, tnear, dp.p, dt.p, de.p, st);
     if (rc == RTG_OK) {
       e = cudaMemcpyAsync(prim_out, dp.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, dt.p, n * sizeof(float), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&errors, de.p, sizeof errors, cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) rc = check_cuda(ctx, e, "trace_rays");
     }
@@ -998,6 +1067,9 @@ int rtg_trace_rays(rtg_context* ctx, const float* rays, int64_t n, float tnear, 
   dfree(dr);
   dfree(dt);
   dfree(dp);
+  dfree(de);
+  if (rc == RTG_OK && errors)
+    rc = set_error(ctx, RTG_ERR_BUDGET, "a device-side traversal limit was reached");
   return rc;
 }
 

@@ -31,6 +31,8 @@ struct Job {
   DBuf<unsigned long long> cnt;
   DBuf<float> areas;
   TraceParams p{};
+  int64_t np = 0;        // primitives of the surface (the size of acc, cnt, areas)
+  uint64_t version = 0;  // the context's version that p was made from
 };
 
 }  // namespace
@@ -83,9 +85,8 @@ int build_tables(rtg_batch* b) {
 int enqueue_batched(rtg_batch* b, cudaStream_t st, const uint64_t* prefix, uint64_t total) {
   rtg_context* ctx = &b->aux;
   for (Job& j : b->jobs) {
-    const int64_t np = j.scene->g.nd + j.scene->g.nt;
-    RTG_CUDA(ctx, cudaMemsetAsync(j.acc.p, 0, 4 * np * sizeof(double), st));
-    RTG_CUDA(ctx, cudaMemsetAsync(j.cnt.p, 0, np * sizeof(unsigned long long), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(j.acc.p, 0, 4 * j.np * sizeof(double), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(j.cnt.p, 0, j.np * sizeof(unsigned long long), st));
   }
   RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
   TraceParams p0{};
@@ -94,6 +95,63 @@ int enqueue_batched(rtg_batch* b, cudaStream_t st, const uint64_t* prefix, uint6
   if (total > 0)
     RTG_TRY(launch_trace_batched(ctx, p0, b->d_jobs.p, prefix, (int)b->jobs.size(), total, st, ctx->lc, b->depth));
   for (Job& j : b->jobs) RTG_TRY(compute_areas_into(j.scene, st, j.box_lo, j.box_hi, j.areas.p));
+  return RTG_OK;
+}
+
+// What a batch cannot trace (the batched kernel runs rti's neighbour deposit
+// into FP64 accumulators only); nullptr when the context is fine.
+const char* unsupported_mode(const rtg_context* scene) {
+  if (scene->deposit_mode != RTG_DEPOSIT_NEIGHBORS) return "a batch traces the neighbour deposit only";
+  if (scene->accum != RTG_ACCUM_FP64) return "a batch accumulates in FP64 only";
+  return nullptr;
+}
+
+// The kernel parameters of job j from its context's current surface, into
+// the job's own accumulators.
+int prepare_job(rtg_batch* b, Job& j) {
+  rtg_context* ctx = &b->aux;
+  rtg_context* scene = j.scene;
+  box_for(j.cfg, scene->g, j.box_lo, j.box_hi);
+  TraceParams p;
+  const int rc = prepare_trace_with(scene, j.cfg, j.box_lo, j.box_hi, 0, j.n_rays, j.seed, p);
+  if (rc != RTG_OK) return set_error(ctx, rc, rtg_last_error(scene));
+  p.s1 = j.acc.p;
+  p.s2 = j.acc.p + j.np;
+  p.s3 = j.acc.p + 2 * j.np;
+  p.s4 = j.acc.p + 3 * j.np;
+  p.cnt = j.cnt.p;
+  p.tally = ctx->d_tally;
+  p.abort_flag = nullptr;
+  j.p = p;
+  j.version = scene->version;
+  return RTG_OK;
+}
+
+// Before a run: jobs whose context changed since their parameters were made
+// (refit, new tree, sticking field, visit limit, a new upload) are prepared
+// again, and the job table and the captured graph are rebuilt; a job whose
+// surface no longer has the same number of primitives fails the run.
+int refresh_jobs(rtg_batch* b) {
+  rtg_context* ctx = &b->aux;
+  bool changed = false;
+  for (size_t i = 0; i < b->jobs.size(); ++i) {
+    Job& j = b->jobs[i];
+    const rtg_context* scene = j.scene;
+    if (scene->version == j.version) continue;
+    if (scene->g.nd + scene->g.nt != j.np || !scene->g.nodes.p)
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT,
+                       "job " + std::to_string(i) + ": its surface no longer has the same number of primitives");
+    if (const char* why = unsupported_mode(scene))
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "job " + std::to_string(i) + ": " + why);
+    RTG_TRY(prepare_job(b, j));
+    changed = true;
+  }
+  if (changed) {
+    b->depth = 0;
+    for (const Job& j : b->jobs) b->depth = std::max(b->depth, j.scene->g.depth);
+    b->tables_ready = false;
+    drop_graph(b);
+  }
   return RTG_OK;
 }
 
@@ -157,10 +215,7 @@ int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint6
   if (scene->device != ctx->device) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "scene is on another device");
   if (scene->g.nd + scene->g.nt == 0 || !scene->g.nodes.p)
     return set_error(ctx, RTG_ERR_NO_GEOMETRY, "scene has no geometry");
-  if (scene->deposit_mode != RTG_DEPOSIT_NEIGHBORS)
-    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a batch traces the neighbour deposit only");
-  if (scene->accum != RTG_ACCUM_FP64)
-    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "a batch accumulates in FP64 only");
+  if (const char* why = unsupported_mode(scene)) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, why);
   if (b->jobs.size() >= 0x7FFFFFFF) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "too many jobs");
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));
   Job j;
@@ -170,28 +225,17 @@ int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint6
   j.cfg.job = (uint32_t)b->jobs.size();  // a Philox stream of its own
   j.n_rays = n_rays;
   j.seed = seed;
-  box_for(j.cfg, scene->g, j.box_lo, j.box_hi);
-  const int64_t np = scene->g.nd + scene->g.nt;
-  int rc = dalloc(ctx, j.acc, (size_t)(4 * np), "batch accumulators");
-  if (rc == RTG_OK) rc = dalloc(ctx, j.cnt, (size_t)np, "batch counts");
-  if (rc == RTG_OK) rc = dalloc(ctx, j.areas, (size_t)np, "batch areas");
-  if (rc == RTG_OK) {
-    rc = prepare_trace_with(scene, j.cfg, j.box_lo, j.box_hi, 0, n_rays, seed, j.p);
-    if (rc != RTG_OK) set_error(ctx, rc, rtg_last_error(scene));
-  }
+  j.np = scene->g.nd + scene->g.nt;
+  int rc = dalloc(ctx, j.acc, (size_t)(4 * j.np), "batch accumulators");
+  if (rc == RTG_OK) rc = dalloc(ctx, j.cnt, (size_t)j.np, "batch counts");
+  if (rc == RTG_OK) rc = dalloc(ctx, j.areas, (size_t)j.np, "batch areas");
+  if (rc == RTG_OK) rc = prepare_job(b, j);
   if (rc != RTG_OK) {
     dfree(j.acc);
     dfree(j.cnt);
     dfree(j.areas);
     return rc;
   }
-  j.p.s1 = j.acc.p;
-  j.p.s2 = j.acc.p + np;
-  j.p.s3 = j.acc.p + 2 * np;
-  j.p.s4 = j.acc.p + 3 * np;
-  j.p.cnt = j.cnt.p;
-  j.p.tally = ctx->d_tally;
-  j.p.abort_flag = nullptr;
   b->jobs.push_back(j);
   if (scene->g.depth > b->depth) b->depth = scene->g.depth;
   b->tables_ready = false;
@@ -210,6 +254,7 @@ int rtg_batch_run(rtg_batch* b, int use_graph, void* stream) {
   if (!b) return RTG_ERR_INVALID_ARGUMENT;
   rtg_context* ctx = &b->aux;
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  RTG_TRY(refresh_jobs(b));
   if (!b->tables_ready) RTG_TRY(build_tables(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   RTG_CUDA(ctx, cudaEventRecord(b->ev0, st));
@@ -241,13 +286,13 @@ int rtg_batch_run_sequential(rtg_batch* b, void* stream) {
   if (!b) return RTG_ERR_INVALID_ARGUMENT;
   rtg_context* ctx = &b->aux;
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  RTG_TRY(refresh_jobs(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   RTG_CUDA(ctx, cudaEventRecord(b->ev0, st));
   RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
   for (Job& j : b->jobs) {
-    const int64_t np = j.scene->g.nd + j.scene->g.nt;
-    RTG_CUDA(ctx, cudaMemsetAsync(j.acc.p, 0, 4 * np * sizeof(double), st));
-    RTG_CUDA(ctx, cudaMemsetAsync(j.cnt.p, 0, np * sizeof(unsigned long long), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(j.acc.p, 0, 4 * j.np * sizeof(double), st));
+    RTG_CUDA(ctx, cudaMemsetAsync(j.cnt.p, 0, j.np * sizeof(unsigned long long), st));
     RTG_CUDA(ctx, cudaMemsetAsync(&ctx->d_tally->next_ray, 0, sizeof(unsigned long long), st));
     if (j.n_rays > 0) {
       const int rc = launch_trace(j.scene, j.p, st, kModeForward);
@@ -279,7 +324,7 @@ int rtg_batch_get_results(rtg_batch* b, int32_t job, double* s1, uint64_t* count
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));
   RTG_CUDA(ctx, cudaDeviceSynchronize());
   Job& j = b->jobs[(size_t)job];
-  const int64_t np = j.scene->g.nd + j.scene->g.nt;
+  const int64_t np = j.np;
   if (s1) RTG_CUDA(ctx, cudaMemcpy(s1, j.acc.p, np * sizeof(double), cudaMemcpyDeviceToHost));
   if (counts) RTG_CUDA(ctx, cudaMemcpy(counts, j.cnt.p, np * sizeof(uint64_t), cudaMemcpyDeviceToHost));
   if (areas) RTG_CUDA(ctx, cudaMemcpy(areas, j.areas.p, np * sizeof(float), cudaMemcpyDeviceToHost));
@@ -328,6 +373,7 @@ int rtg_batch_autotune(rtg_batch* b, double fraction, rtg_launch_config* best, d
   if (!b || !(fraction > 0.0 && fraction <= 1.0)) return RTG_ERR_INVALID_ARGUMENT;
   rtg_context* ctx = &b->aux;
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));
+  RTG_TRY(refresh_jobs(b));
   if (!b->tables_ready) RTG_TRY(build_tables(b));
   const int n = (int)b->jobs.size();
   if (n == 0) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "empty batch");

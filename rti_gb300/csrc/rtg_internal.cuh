@@ -54,6 +54,9 @@ struct SceneView {
   const int64_t* nb_ptr;
   const uint32_t* nb_slot;
   const float* sticking_field;  // by original id or nullptr
+  // node visits after which one closest-hit (or interval) query ends and
+  // counts as an error
+  int64_t max_visits;
 };
 
 struct TraceParams {
@@ -178,6 +181,12 @@ struct rtg_context {
   int32_t deposit_mode = RTG_DEPOSIT_NEIGHBORS;
   int32_t accum = RTG_ACCUM_FP64;
   float window_factor = 5.0f;  // point_cloud_context.hpp:163
+  uint64_t visit_limit = 0;    // 0: 4 x primitives + 64, more than a valid tree needs
+  // bumped whenever the surface's device buffers, its tree or a trace input
+  // that a batch job captured (sticking field, visit limit) may have changed
+  uint64_t version = 0;
+  // fault injection: real device allocations left before one fails (-1: off)
+  int64_t alloc_failure_in = -1;
   rtg::Wavefront wf;
   std::string err;
 };
@@ -208,8 +217,10 @@ int finalize_estimates(rtg_context* ctx, cudaStream_t st);
 int compute_stats(rtg_context* ctx, cudaStream_t st, uint64_t total, double* d_rel, double* d_vov);
 // trace.cu: a single trace with the context's launch configuration
 int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st, int mode = kModeForward);
+// closest hits of explicit rays; queries that reach a traversal limit are
+// counted in *d_errors
 int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim,
-                       float* d_t, cudaStream_t st);
+                       float* d_t, unsigned long long* d_errors, cudaStream_t st);
 SceneView scene_view(rtg_context* ctx);
 // stack entries for a requested depth (0 = automatic) and a tree depth: 32, 64 or 256
 int stack_for(int requested, int tree_depth);
@@ -232,11 +243,21 @@ int compute_areas_into(rtg_context* ctx, cudaStream_t st, const float* box_lo, c
 
 // api.cu helpers
 int check_config(rtg_context* ctx, const rtg_config& c);
+// Frees the surface after a failed upload, update or rebuild (whose buffers
+// may no longer agree with one another): later traces report
+// RTG_ERR_NO_GEOMETRY until an upload succeeds.
+void drop_surface(rtg_context* ctx);
 void box_for(const rtg_config& c, const Geometry& g, float* box_lo, float* box_hi);
 int prepare_trace_with(rtg_context* ctx, const rtg_config& c, const float* box_lo, const float* box_hi,
                        uint64_t ray_begin, uint64_t ray_end, uint64_t seed, TraceParams& p);
 int set_error(rtg_context* ctx, int code, const std::string& msg);
 int check_cuda(rtg_context* ctx, cudaError_t e, const char* what);
+// Fault injection (rtg_inject_alloc_failure): whether this allocation is the
+// one chosen to fail.
+inline bool injected_alloc_failure(rtg_context* ctx) {
+  if (ctx->alloc_failure_in < 0) return false;
+  return ctx->alloc_failure_in-- == 0;  // fails once, then -1 (off)
+}
 template <typename T>
 int dalloc(rtg_context* ctx, DBuf<T>& b, size_t n, const char* what) {
   if (b.p && b.n >= n && n > 0) {
@@ -247,6 +268,8 @@ int dalloc(rtg_context* ctx, DBuf<T>& b, size_t n, const char* what) {
   b.p = nullptr;
   b.n = 0;
   if (n == 0) return RTG_OK;
+  if (injected_alloc_failure(ctx))
+    return set_error(ctx, RTG_ERR_OUT_OF_MEMORY, std::string("cudaMalloc failed for ") + what + " (injected)");
   cudaError_t e = cudaMalloc((void**)&b.p, n * sizeof(T));
   if (e != cudaSuccess) {
     b.p = nullptr;
@@ -270,6 +293,8 @@ int talloc(rtg_context* ctx, DBuf<T>& b, size_t n, cudaStream_t st, const char* 
   b.p = nullptr;
   b.n = 0;
   if (n == 0) return RTG_OK;
+  if (injected_alloc_failure(ctx))
+    return set_error(ctx, RTG_ERR_OUT_OF_MEMORY, std::string("cudaMallocAsync failed for ") + what + " (injected)");
   cudaError_t e = cudaMallocAsync((void**)&b.p, n * sizeof(T), st);
   if (e != cudaSuccess) {
     b.p = nullptr;

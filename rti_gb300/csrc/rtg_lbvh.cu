@@ -570,6 +570,7 @@ int build_ploc(rtg_context* ctx, const uint32_t* d_sorted_prim, cudaStream_t st)
       ploc_flags_kernel<<<blocks_for(bound, 256), 256, 0, st>>>(nn.p, bound, state.p,
                                                                 (unsigned long long*)packed.p);
       rc = exclusive_scan_i64(ctx, packed.p, bound, total.p, st);
+      if (rc != RTG_OK) break;
       ploc_merge_kernel<<<blocks_for(bound, 256), 256, 0, st>>>(
           nn.p, bound, state.p, cid[q].p, blo[q].p, bhi[q].p, (const unsigned long long*)packed.p, n_int,
           g.leaf_ref.p, n, g.nodes.p, g.parent.p, cid[q ^ 1].p, blo[q ^ 1].p, bhi[q ^ 1].p);
@@ -625,11 +626,15 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
     return RTG_OK;
   }
   DBuf<float> node_box;
-  RTG_TRY(talloc(ctx, node_box, (size_t)(6 * (np - 1)), st, "node boxes"));
   DBuf<unsigned long long> err;
-  int rc = talloc(ctx, err, 1, st, "refit status");
-  if (rc != RTG_OK) { tfree(node_box, st); return rc; }
-  RTG_TRY(dalloc(ctx, g.refit_flags, (size_t)(np - 1), "refit flags"));
+  int rc = talloc(ctx, node_box, (size_t)(6 * (np - 1)), st, "node boxes");
+  if (rc == RTG_OK) rc = talloc(ctx, err, 1, st, "refit status");
+  if (rc == RTG_OK) rc = dalloc(ctx, g.refit_flags, (size_t)(np - 1), "refit flags");
+  if (rc != RTG_OK) {
+    tfree(node_box, st);
+    tfree(err, st);
+    return rc;
+  }
   cudaMemsetAsync(g.refit_flags.p, 0, sizeof(unsigned int) * (np - 1), st);
   cudaMemsetAsync(err.p, 0, sizeof(unsigned long long), st);
   refit_kernel<<<blocks_for(np, 256), 256, 0, st>>>(np, g.leaf_ref.p, g.parent.p, g.disc.p, g.tri.p,
@@ -699,7 +704,12 @@ int build_lbvh(rtg_context* ctx) {
         cudaMemsetAsync(g.parent.p, 0xFF, 2 * np * sizeof(uint32_t), st);
         if ((rc = build_ploc(ctx, vals.p, st)) != RTG_OK) break;
         if ((rc = validate_tree(ctx, st)) != RTG_OK) break;
-        karras = tree_depth(ctx, st) != RTG_OK;
+        const int drc = tree_depth(ctx, st);  // RTG_ERR_INTERNAL: too deep for the stacks
+        if (drc != RTG_OK && drc != RTG_ERR_INTERNAL) {
+          rc = drc;
+          break;
+        }
+        karras = drc != RTG_OK;
       }
       if (karras) {
         cudaMemsetAsync(g.parent.p, 0xFF, 2 * np * sizeof(uint32_t), st);

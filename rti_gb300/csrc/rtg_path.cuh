@@ -133,7 +133,7 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   auto stack = [&](int i) -> uint32_t& { return SST ? sstk[i * SST] : lstack[i]; };
   int sp = 0;
   uint32_t cur = s.root;
-  const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
+  const int64_t max_iter = s.max_visits;
   if (!POSTPONE) {
     for (int64_t it = 0;; ++it) {
       if (it > max_iter) {
@@ -279,7 +279,7 @@ __device__ void leaves_in_interval(const SceneView& s, const Ray& r, float tlo, 
   uint32_t stack[STACK];
   int sp = 0;
   uint32_t cur = s.root;
-  const int64_t max_iter = 4 * (int64_t)(s.nd + s.nt) + 64;
+  const int64_t max_iter = s.max_visits;
   for (int64_t it = 0;; ++it) {
     if (it > max_iter) {
       errs += 1;

@@ -1,5 +1,7 @@
 // rtg_trace.cu -- launches of the path kernel for one context (forward trace
 // and adjoint replays), and the explicit-ray closest-hit kernel.
+#include <algorithm>
+
 #include "rtg_path.cuh"
 
 namespace rtg {
@@ -138,6 +140,8 @@ SceneView scene_view(rtg_context* ctx) {
   s.nb_ptr = g.nd > 0 ? g.nb_ptr.p : nullptr;
   s.nb_slot = g.nb_slot.p;
   s.sticking_field = ctx->sticking_field.p;
+  const int64_t automatic = 4 * (int64_t)(g.nd + g.nt) + 64;
+  s.max_visits = ctx->visit_limit ? (int64_t)std::min<uint64_t>(ctx->visit_limit, (uint64_t)automatic) : automatic;
   return s;
 }
 
@@ -177,11 +181,10 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
 }
 
 int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim, float* d_t,
-                       cudaStream_t st) {
+                       unsigned long long* d_errors, cudaStream_t st) {
   if (n <= 0) return RTG_OK;
   SceneView s = scene_view(ctx);
-  closest_hit_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, d_rays, n, tnear, d_prim, d_t,
-                                                                   &ctx->d_tally->errors);
+  closest_hit_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, d_rays, n, tnear, d_prim, d_t, d_errors);
   RTG_CUDA(ctx, cudaGetLastError());
   return RTG_OK;
 }

@@ -305,6 +305,7 @@ int launch_wavefront(rtg_context* ctx, const TraceParams& p0, const TraceParams*
   constexpr uint64_t kMaxCapacity = 1u << 20;
   uint64_t cap = std::min<uint64_t>(kMaxCapacity, (total_rays + 1023) / 1024 * 1024);
   if (wf.capacity < cap) {
+    wf.capacity = 0;  // until every queue has the new size (an allocation may fail half way)
     for (int q = 0; q < 2; ++q) {
       RTG_TRY(dalloc(ctx, wf.ow[q], (size_t)cap, "wavefront queue"));
       RTG_TRY(dalloc(ctx, wf.dk[q], (size_t)cap, "wavefront queue"));

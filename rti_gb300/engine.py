@@ -203,6 +203,21 @@ class Engine:
     def set_accumulation(self, mode: int):
         self._check(self._L.rtg_set_accumulation(self._h, int(mode)))
 
+    @property
+    def visit_limit(self) -> int:
+        """Node visits per closest-hit query before it ends as an error (0: automatic)."""
+        v = C.c_uint64()
+        self._check(self._L.rtg_get_visit_limit(self._h, C.byref(v)))
+        return v.value
+
+    def set_visit_limit(self, visits: int):
+        self._check(self._L.rtg_set_visit_limit(self._h, int(visits)))
+
+    def inject_alloc_failure(self, after: int):
+        """Test hook: the device allocation after ``after`` more successful ones
+        fails as if the device were out of memory (once); negative cancels."""
+        self._check(self._L.rtg_inject_alloc_failure(self._h, int(after)))
+
     def set_deposit_mode(self, mode: int, window_factor: float = 5.0):
         """Selects the deposit of a front-face disc hit for later traces."""
         self._check(self._L.rtg_set_deposit_mode(self._h, int(mode), float(window_factor)))

@@ -273,6 +273,52 @@ def test_abort_returns_status(eng, trench):
     eng.configure(sticking=0.1)
 
 
+def test_visit_limit_returns_budget_error(eng, trench):
+    """A closest-hit query that reaches the node-visit limit ends and is
+    counted; the getters of that trace return RTG_ERR_BUDGET (5) in every
+    schedule, as do explicit rays, the adjoint and a batch; the context stays
+    usable, and with the limit lifted it traces exactly as before."""
+    from rti_gb300 import RtgError
+    from rti_gb300 import _lib as L
+    from rti_gb300.batch import Batch
+    _upload_discs(eng, trench, sticking=0.1, x_bound=1, y_bound=1)
+    n = 20000
+    ref = _gpu_trace(eng, n, seed=4)
+    rays = _random_rays(2000, np.array(trench.box_lo, np.float32), np.array(trench.box_hi, np.float32), 1)
+    prim_ref, t_ref = eng.trace_rays(rays)
+    eng.set_visit_limit(1 << 40)  # capped at the automatic limit: no change
+    assert np.array_equal(_gpu_trace(eng, n, seed=4)["counts"], ref["counts"])
+    eng.set_visit_limit(3)
+    assert eng.visit_limit == 3
+    for sched in (L.RTG_SCHED_MEGAKERNEL, L.RTG_SCHED_WAVEFRONT, L.RTG_SCHED_PLAIN):
+        eng.set_launch_config(scheduling=sched)
+        eng.trace(n, 4)
+        with pytest.raises(RtgError) as ei:
+            eng.hit_counts()
+        assert ei.value.code == L.RTG_ERR_BUDGET
+        t = eng.tally()
+        assert 0 < t.errors <= t.segments
+    eng.set_launch_config()
+    with pytest.raises(RtgError) as ei:
+        eng.trace_rays(rays)
+    assert ei.value.code == L.RTG_ERR_BUDGET
+    with pytest.raises(RtgError) as ei:
+        eng.adjoint(np.ones(trench.n), n, seed=4)
+    assert ei.value.code == L.RTG_ERR_BUDGET
+    with Batch(0) as b:
+        b.add(eng, n, seed=4)
+        b.run(use_graph=False)
+        with pytest.raises(RtgError) as ei:
+            b.synchronize()
+        assert ei.value.code == L.RTG_ERR_BUDGET
+    eng.set_visit_limit(0)
+    again = _gpu_trace(eng, n, seed=4)
+    assert np.array_equal(again["counts"], ref["counts"])
+    assert again["tally"].errors == 0 and again["tally"].segments == ref["tally"].segments
+    prim, t = eng.trace_rays(rays)
+    assert np.array_equal(prim, prim_ref) and np.array_equal(t, t_ref)
+
+
 def test_independent_streams_agree_within_4_sigma(eng, trench, oracle_lib):
     """GPU (seed 100) and oracle (seed 200) are independent Monte Carlo runs:
     the flux summed over 25 depth bands must agree within 4 sigma, sigma from
