@@ -406,10 +406,14 @@ int build_neighbors(rtg_context* ctx) {
     cudaMemsetAsync(counts.p + nd, 0, sizeof(int64_t), st);
     int64_t* total = g.nb_ptr.p + nd;
     if ((rc = exclusive_scan_i64(ctx, counts.p, nd + 1, nullptr, st)) != RTG_OK) break;
-    RTG_CUDA(ctx, cudaMemcpyAsync(g.nb_ptr.p, counts.p, (nd + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
     int64_t nnz = 0;
-    RTG_CUDA(ctx, cudaMemcpyAsync(&nnz, total, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    RTG_CUDA(ctx, cudaStreamSynchronize(st));
+    cudaError_t ce = cudaMemcpyAsync(g.nb_ptr.p, counts.p, (nd + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&nnz, total, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) {
+      rc = check_cuda(ctx, ce, "neighbour counts");
+      break;
+    }
     g.nb_nnz = nnz;
     if ((rc = dalloc(ctx, g.nb_idx, (size_t)(nnz > 0 ? nnz : 1), "neighbour columns")) != RTG_OK) break;
     neighbor_kernel<true><<<blocks_for(nd, 128), 128, 0, st>>>(g.disc_cr_by_id.p, nd, grid, vals.p, cs.p, ce.p,
