@@ -407,11 +407,11 @@ int build_neighbors(rtg_context* ctx) {
     int64_t* total = g.nb_ptr.p + nd;
     if ((rc = exclusive_scan_i64(ctx, counts.p, nd + 1, nullptr, st)) != RTG_OK) break;
     int64_t nnz = 0;
-    cudaError_t ce = cudaMemcpyAsync(g.nb_ptr.p, counts.p, (nd + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, st);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&nnz, total, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-    if (ce != cudaSuccess) {
-      rc = check_cuda(ctx, ce, "neighbour counts");
+    cudaError_t cerr = cudaMemcpyAsync(g.nb_ptr.p, counts.p, (nd + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, st);
+    if (cerr == cudaSuccess) cerr = cudaMemcpyAsync(&nnz, total, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (cerr == cudaSuccess) cerr = cudaStreamSynchronize(st);
+    if (cerr != cudaSuccess) {
+      rc = check_cuda(ctx, cerr, "neighbour counts");
       break;
     }
     g.nb_nnz = nnz;
