@@ -56,7 +56,7 @@ struct SceneView {
   const float* sticking_field;  // by original id or nullptr
   // node visits after which one closest-hit (or interval) query ends and
   // counts as an error
-  int64_t max_visits;
+  uint32_t max_visits;
 };
 
 struct TraceParams {

@@ -133,10 +133,10 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   auto stack = [&](int i) -> uint32_t& { return SST ? sstk[i * SST] : lstack[i]; };
   int sp = 0;
   uint32_t cur = s.root;
-  const int64_t max_iter = s.max_visits;
+  const uint32_t max_iter = s.max_visits;
   if (!POSTPONE) {
-    for (int64_t it = 0;; ++it) {
-      if (it > max_iter) {
+    for (uint32_t it = 0;; ++it) {
+      if (it >= max_iter) {
         errs += 1;
         break;
       }
@@ -187,12 +187,12 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   // while-while: leaves travel through `cur` and the stack like inner nodes
   constexpr uint32_t kNone = 0xFFFFFFFFu;
   uint32_t leaf = kNone;
-  int64_t it = 0;
+  uint32_t it = 0;
   auto pop = [&]() -> uint32_t { return sp > 0 ? stack(--sp) : kNone; };
   while (cur != kNone) {
     // inner nodes until every lane of the warp holds a pending leaf
     while (cur != kNone && !(cur & kLeafBit)) {
-      if (++it > max_iter) {
+      if (it++ >= max_iter) {
         errs += 1;
         cur = kNone;
         break;
@@ -228,7 +228,7 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
     }
     // the pending leaf, and any leaf reached right after it
     while (leaf != kNone) {
-      if (++it > max_iter) {
+      if (it++ >= max_iter) {
         errs += 1;
         cur = kNone;
         break;
@@ -279,9 +279,9 @@ __device__ void leaves_in_interval(const SceneView& s, const Ray& r, float tlo, 
   uint32_t stack[STACK];
   int sp = 0;
   uint32_t cur = s.root;
-  const int64_t max_iter = s.max_visits;
-  for (int64_t it = 0;; ++it) {
-    if (it > max_iter) {
+  const uint32_t max_iter = s.max_visits;
+  for (uint32_t it = 0;; ++it) {
+    if (it >= max_iter) {
       errs += 1;
       return;
     }

@@ -140,8 +140,9 @@ SceneView scene_view(rtg_context* ctx) {
   s.nb_ptr = g.nd > 0 ? g.nb_ptr.p : nullptr;
   s.nb_slot = g.nb_slot.p;
   s.sticking_field = ctx->sticking_field.p;
-  const int64_t automatic = 4 * (int64_t)(g.nd + g.nt) + 64;
-  s.max_visits = ctx->visit_limit ? (int64_t)std::min<uint64_t>(ctx->visit_limit, (uint64_t)automatic) : automatic;
+  // a valid query visits each node at most once (< 2 x primitives)
+  const uint64_t automatic = std::min<uint64_t>(4 * (uint64_t)(g.nd + g.nt) + 64, 0xFFFFFFFFull);
+  s.max_visits = (uint32_t)(ctx->visit_limit ? std::min<uint64_t>(ctx->visit_limit, automatic) : automatic);
   return s;
 }
 
