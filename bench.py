@@ -55,8 +55,16 @@ def workload():
                                  jitter=0.01, seed=0, source_gap=0.1)
 
 
+TREE = "karras"  # --tree
+
+
+def set_tree(name):
+    global TREE
+    TREE = name
+
+
 def config_dict(h, n_rays):
-    return {"workload": "hole_triangles", "radius": 0.5, "depth": 10.0, "cell": "2x2 periodic",
+    return {"workload": "hole_triangles", "radius": 0.5, "depth": 10.0, "cell": "2x2 periodic", "tree": TREE,
             "n_triangles": int(h.n), "n_rays_per_step": int(n_rays), "sticking": STICKING,
             "specular_fraction": SPECULAR, "source_exponent": 1.0, "source_plane_z": 0.1,
             "l2": "flushed between steps (256 MB write)", "parallelism": "rays sharded per rank (weak scaling)"}
@@ -354,6 +362,7 @@ def run_ours(args):
     import torch.distributed as dist
 
     from rti_gb300 import Engine
+    from rti_gb300 import _lib as L
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -365,6 +374,8 @@ def run_ours(args):
     h = workload()
     R = args.rays
     eng = Engine(local)
+    tree = L.RTG_TREE_PLOC if TREE == "ploc" else L.RTG_TREE_KARRAS
+    eng.set_tree_builder(tree)
     eng.upload_triangles(h.vertices, h.indices)
     eng.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
                   x_bound=1, y_bound=1, source_exponent=1.0)
@@ -452,6 +463,7 @@ def run_ours(args):
         pin_c = torch.zeros(h.n, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
         pin_s = torch.zeros(h.n, dtype=torch.float64).pin_memory().numpy()
         def e2e_step(e2, k):
+            e2.set_tree_builder(tree)
             e2.upload_triangles(pin_v, pin_i)
             e2.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
                          x_bound=1, y_bound=1)
@@ -614,11 +626,13 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-rays", type=int, default=2_000_000, help="rays per job of the batch block")
     ap.add_argument("--no-rough", action="store_true")
+    ap.add_argument("--tree", default=TREE, choices=["karras", "ploc"], help="tree builder of the hole")
     ap.add_argument("--sweep", default="", help="comma-separated ray counts: path-kernel time against rays "
                                                 "(the tail analysis), printed instead of the bench line")
     ap.add_argument("--rough-rays", type=int, default=100_000_000, help="rays of the rough-surface block")
     ap.add_argument("--rough-only", action="store_true", help="run the rough-surface block alone and print it")
     args = ap.parse_args()
+    set_tree(args.tree)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     from __graft_entry__ import build
     if args.impl == "reference":
