@@ -73,73 +73,127 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter(const uint32_t* __restr
   }
 }
 
-// Single-block exclusive scan, in place, in chunks of blockDim*4 items.
+constexpr int kScanThreads = 1024;
+constexpr int64_t kScanChunk = (int64_t)kScanThreads * 4;  // items one block scans in one step
+
+// Exclusive scan of items [base, base + kScanChunk) of a, in place, after
+// `carry`; returns the chunk's total.  All threads of the block call it.
 template <typename T>
-__global__ void __launch_bounds__(1024) scan_excl_kernel(T* __restrict__ a, int64_t m, T* total) {
-  __shared__ T warp_sums[32];
-  __shared__ T carry_s;
+__device__ T scan_chunk(T* __restrict__ a, int64_t base, int64_t m, T carry, T* warp_sums) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nw = blockDim.x >> 5;
-  if (tid == 0) carry_s = 0;
-  __syncthreads();
-  const int64_t chunk = (int64_t)blockDim.x * 4;
-  for (int64_t base = 0; base < m; base += chunk) {
-    T v[4];
-    T s = 0;
+  T v[4];
+  T s = 0;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int64_t i = base + (int64_t)tid * 4 + q;
-      v[q] = i < m ? a[i] : (T)0;
-      s += v[q];
-    }
-    // inclusive warp scan of the thread sums
-    T x = s;
+  for (int q = 0; q < 4; ++q) {
+    const int64_t i = base + (int64_t)tid * 4 + q;
+    v[q] = i < m ? a[i] : (T)0;
+    s += v[q];
+  }
+  // inclusive warp scan of the thread sums
+  T x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < nw ? warp_sums[lane] : (T)0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      T y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-      if (lane >= o) x += y;
+      T y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
     }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      T w = lane < nw ? warp_sums[lane] : (T)0;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        T y = __shfl_up_sync(0xFFFFFFFFu, w, o);
-        if (lane >= o) w += y;
-      }
-      if (lane < nw) warp_sums[lane] = w;
-    }
-    __syncthreads();
-    const T carry = carry_s;
-    T excl = carry + (warp > 0 ? warp_sums[warp - 1] : (T)0) + (x - s);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int64_t i = base + (int64_t)tid * 4 + q;
-      if (i < m) a[i] = excl;
-      excl += v[q];
-    }
-    __syncthreads();
-    if (tid == 0) carry_s = carry + warp_sums[nw - 1];
-    __syncthreads();
+    if (lane < nw) warp_sums[lane] = w;
   }
-  if (tid == 0 && total) *total = carry_s;
+  __syncthreads();
+  T excl = carry + (warp > 0 ? warp_sums[warp - 1] : (T)0) + (x - s);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int64_t i = base + (int64_t)tid * 4 + q;
+    if (i < m) a[i] = excl;
+    excl += v[q];
+  }
+  const T chunk_total = warp_sums[nw - 1];
+  __syncthreads();  // warp_sums is reused by the next call
+  return chunk_total;
+}
+
+// Single-block exclusive scan, in place, chunk after chunk.
+template <typename T>
+__global__ void __launch_bounds__(kScanThreads) scan_excl_kernel(T* __restrict__ a, int64_t m, T* total) {
+  __shared__ T warp_sums[32];
+  T carry = 0;
+  for (int64_t base = 0; base < m; base += kScanChunk) carry += scan_chunk(a, base, m, carry, warp_sums);
+  if (threadIdx.x == 0 && total) *total = carry;
+}
+
+// Multi-block scan, pass 1: the total of every chunk.
+template <typename T>
+__global__ void __launch_bounds__(kScanThreads) chunk_sum_kernel(const T* __restrict__ a, int64_t m,
+                                                                 T* __restrict__ sums) {
+  __shared__ T warp_sums[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk;
+  T s = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int64_t i = base + (int64_t)tid * 4 + q;
+    if (i < m) s += a[i];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+  if (lane == 0) warp_sums[warp] = s;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : (T)0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xFFFFFFFFu, w, o);
+    if (lane == 0) sums[blockIdx.x] = w;
+  }
+}
+
+// Multi-block scan, pass 3: every chunk after its scanned offset (pass 2 is
+// scan_excl_kernel over the chunk totals).
+template <typename T>
+__global__ void __launch_bounds__(kScanThreads) chunk_scan_kernel(T* __restrict__ a, int64_t m,
+                                                                  const T* __restrict__ offsets) {
+  __shared__ T warp_sums[32];
+  scan_chunk(a, (int64_t)blockIdx.x * kScanChunk, m, offsets[blockIdx.x], warp_sums);
+}
+
+// Exclusive scan of m items in place (total into *d_total when given): one
+// block for short arrays, three passes over chunks of kScanChunk otherwise.
+template <typename T>
+int exclusive_scan(rtg_context* ctx, T* d_a, int64_t m, T* d_total, cudaStream_t st) {
+  if (m <= 0) return RTG_OK;
+  if (m <= 4 * kScanChunk) {
+    scan_excl_kernel<T><<<1, kScanThreads, 0, st>>>(d_a, m, d_total);
+    RTG_CUDA(ctx, cudaGetLastError());
+    return RTG_OK;
+  }
+  const int64_t nc = (m + kScanChunk - 1) / kScanChunk;
+  DBuf<T> sums;
+  RTG_TRY(talloc(ctx, sums, (size_t)nc, st, "scan chunk totals"));
+  chunk_sum_kernel<T><<<(unsigned)nc, kScanThreads, 0, st>>>(d_a, m, sums.p);
+  scan_excl_kernel<T><<<1, kScanThreads, 0, st>>>(sums.p, nc, d_total);
+  chunk_scan_kernel<T><<<(unsigned)nc, kScanThreads, 0, st>>>(d_a, m, sums.p);
+  const cudaError_t e = cudaGetLastError();
+  tfree(sums, st);
+  if (e != cudaSuccess) return check_cuda(ctx, e, "scan");
+  return RTG_OK;
 }
 
 }  // namespace
 
 int exclusive_scan_u32(rtg_context* ctx, uint32_t* d_a, int64_t m, uint32_t* d_total, cudaStream_t st) {
-  if (m <= 0) return RTG_OK;
-  scan_excl_kernel<uint32_t><<<1, 1024, 0, st>>>(d_a, m, d_total);
-  RTG_CUDA(ctx, cudaGetLastError());
-  return RTG_OK;
+  return exclusive_scan<uint32_t>(ctx, d_a, m, d_total, st);
 }
 
 int exclusive_scan_i64(rtg_context* ctx, int64_t* d_a, int64_t m, int64_t* d_total, cudaStream_t st) {
-  if (m <= 0) return RTG_OK;
-  scan_excl_kernel<long long><<<1, 1024, 0, st>>>((long long*)d_a, m, (long long*)d_total);
-  RTG_CUDA(ctx, cudaGetLastError());
-  return RTG_OK;
+  return exclusive_scan<long long>(ctx, (long long*)d_a, m, (long long*)d_total, st);
 }
 
 // Sorts (keys, vals) by the low `bits` bits of the keys, stably.  Results end
