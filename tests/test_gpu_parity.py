@@ -138,6 +138,37 @@ def test_neighbors_random_cloud(eng, oracle_lib):
     assert np.array_equal(rg, rc) and np.array_equal(cg, cc)
 
 
+@pytest.mark.parametrize("builder", ["karras", "ploc"])
+def test_large_surface_matches_oracle(eng, oracle_lib, builder):
+    """70 000 discs on a bumpy plane: the build's scans (disc ranks, neighbour
+    counts, PLOC compaction) run as multi-block passes; neighbour lists and
+    the traced hits equal the oracle's under either tree."""
+    from rti_gb300 import _lib as L
+    rng = np.random.default_rng(8)
+    side = 265
+    g1 = (np.arange(side) + 0.5) * (2.0 / side)
+    X, Y = np.meshgrid(g1, g1, indexing="ij")
+    Z = 0.05 * np.sin(7 * X) * np.cos(5 * Y) + 0.01 * rng.standard_normal(X.shape)
+    p = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1).astype(np.float32)
+    nrm = np.tile(np.float32([0, 0, 1]), (len(p), 1))
+    r = np.full(len(p), np.float32(1.1 * 2.0 / side), np.float32)
+    assert len(p) > 4 * 16384
+    eng.set_tree_builder(L.RTG_TREE_PLOC if builder == "ploc" else L.RTG_TREE_KARRAS)
+    try:
+        eng.upload_discs(p, nrm, r)
+        lo, hi = np.float32([0, 0, -0.2]), np.float32([2, 2, 0.2])
+        eng.configure(box=((0, 0, -0.2), (2, 2, 0.2)), sticking=0.3, x_bound=1, y_bound=1, reset=True)
+        g = _gpu_trace(eng, 30000, seed=5)
+        rg, cg = eng.neighbors()
+        s = oracle_lib.Scene(np.concatenate([p, r[:, None]], 1), nrm)
+        rc, cc = s.neighbors()
+        assert np.array_equal(rg, rc) and np.array_equal(cg, cc)
+        c = s.trace(oracle_lib.make_config(lo, hi, sticking=0.3, x_bound=1, y_bound=1, seed=5), 0, 30000)
+        _compare_trace(g, c, len(p))
+    finally:
+        eng.set_tree_builder(L.RTG_TREE_KARRAS)
+
+
 @pytest.mark.parametrize("bound", [1, 0], ids=["periodic", "reflective"])
 def test_trace_trench_matches_oracle(eng, trench, oracle_lib, bound):
     _upload_discs(eng, trench, sticking=0.1, x_bound=bound, y_bound=bound)
