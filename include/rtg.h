@@ -248,7 +248,9 @@ RTG_API int rtg_get_visit_limit(const rtg_context* ctx, uint64_t* visits);
  * context as it was. */
 RTG_API int rtg_inject_alloc_failure(rtg_context* ctx, int64_t after);
 /* Autotuner: for each tree builder (RTG_TREE_*), times each candidate launch
- * configuration (block size x packet x stack depth x scheduling) on source
+ * configuration (block size x packet x stack depth x leaf tests, megakernel
+ * or plain; the wavefront schedule, slower on every workload measured, is
+ * left to rtg_set_launch_config) on source
  * rays [0, sample_rays) with `seed` under the current surface and
  * configuration; keeps the fastest pair as the context's tree and launch
  * configuration and returns the latter (best and best_rays_per_s may be NULL;
@@ -313,14 +315,17 @@ RTG_API int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols,
 
 /* No counterpart in the reference.  The estimates of rtg_get_mc_estimates,
  * written to a device buffer the caller owns (d_out, one float per primitive),
- * enqueued on `stream` (NULL = the context's stream) after the trace and
- * without allocating or freeing any device memory -- for callers whose GPU
- * memory belongs to their own pool, or who cannot take the device-wide
- * synchronisation that cudaFree implies.  Scratch is a fixed 256 KiB array in
- * the library (at most 8388352 primitives; larger surfaces are rejected).
- * The first call on a device looks that array up and should come before any
- * stream capture.  Calls share the array: calls that overlap on the GPU race.
- * The trace's status is not checked here (see rtg_get_tally). */
+ * enqueued on `stream` (NULL = the context's stream) without allocating or
+ * freeing any device memory -- for callers whose GPU memory belongs to their
+ * own pool, or who cannot take the device-wide synchronisation that cudaFree
+ * implies.  The kernels wait (on the GPU, the host does not block) for the end
+ * of the last trace, whichever stream it was enqueued on.  Scratch is a fixed
+ * 256 KiB array in the library (at most 8388352 primitives; larger surfaces
+ * are rejected with RTG_ERR_INVALID_ARGUMENT).  The first call on a device
+ * (and the first after its context was reset) looks that array up and should
+ * come before any stream capture.  Calls share the array: calls that overlap
+ * on the GPU race.  The trace's status is not checked here (see
+ * rtg_get_tally). */
 RTG_API int rtg_get_mc_estimates_noalloc(rtg_context* ctx, float* d_out, void* stream);
 
 /* VTK XML output (rti io/vtp_writer.hpp:27-139, 392-413, without VTK): an
@@ -415,7 +420,8 @@ RTG_API int rtg_batch_get_tally(rtg_batch* b, rtg_tally* out);
  * and is never captured: with it, rtg_batch_run(use_graph != 0) runs uncaptured. */
 RTG_API int rtg_batch_set_launch_config(rtg_batch* b, const rtg_launch_config* lc);
 RTG_API int rtg_batch_get_launch_config(const rtg_batch* b, rtg_launch_config* lc);
-/* Autotuner of the batched launch: times the candidates on the first
+/* Autotuner of the batched launch: times the candidates of rtg_autotune (no
+ * wavefront, so the pick is always graph-captured) on the first
  * sample_fraction (0 < f <= 1) of every job's rays, keeps the fastest. */
 RTG_API int rtg_batch_autotune(rtg_batch* b, double sample_fraction, rtg_launch_config* best,
                                double* best_rays_per_s);

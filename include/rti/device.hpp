@@ -21,9 +21,11 @@
 //     (rti::reflection::diffuse / specular / mixed below, or any type providing
 //     `static constexpr int rtg_mode` and `static constexpr float
 //     rtg_specular_fraction`);
-//   * set(direction) takes effect (cosine_direction_z or
-//     power_cosine_direction_z); in the reference it leaves the cosine source
-//     in place (device.hpp:77-80, 295-296);
+//   * set(direction) changes nothing, as in the reference: there it assigns
+//     through a reference member bound to the cosine source, which copies
+//     only the (empty) i_direction base, so the cosine source stays
+//     (device.hpp:77-80, 295-296).  A cos^n source is selected by the
+//     extension set_source_exponent(n) instead;
 //   * errors throw std::runtime_error with librtg's message, where the
 //     reference asserts;
 //   * extra getters: get_values() (raw S1 per disc, FP64), get_relative_error(),
@@ -206,7 +208,15 @@ class device final {
   void set_number_of_rays(size_t numofrays_) { numofrays = numofrays_; }
   void set_x(bound_condition cond) { xCond = cond; }
   void set_y(bound_condition cond) { yCond = cond; }
-  void set(ray::i_direction<numeric_type>& srcDirection) { exponent = srcDirection.rtg_exponent(); }
+  // The reference's set() leaves its cosine source in place (an assignment
+  // through a reference member that copies only the i_direction base); so
+  // does this one, so that a simulator's flux does not change when it
+  // switches to this header.
+  void set(ray::i_direction<numeric_type>& srcDirection) { (void)srcDirection; }
+  // Extension (no counterpart in the reference): the source emits with
+  // density cos^n of the polar angle (power_cosine_direction_z), n >= 0;
+  // default 1 (cosine_direction_z).
+  void set_source_exponent(numeric_type n) { exponent = n; }
   void set_seed(uint64_t s) { seed = s; }
   void set_cuda_device(int d) { cuda_device = d; }
   // rti's other treatment of overlapping discs, the multi-hit window of

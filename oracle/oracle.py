@@ -91,6 +91,9 @@ def lib():
         L.orc_adjoint.restype = C.c_int
         L.orc_adjoint.argtypes = [C.c_void_p, C.POINTER(OrcConfig), C.c_uint64, C.c_uint64, C.c_int, _f64p, C.c_int,
                                   _f64p, _f64p, _u64p]
+        L.orc_fd_pair.restype = C.c_int
+        L.orc_fd_pair.argtypes = [C.c_void_p, C.POINTER(OrcConfig), C.c_uint64, C.c_uint64, C.c_int, _f64p,
+                                  C.c_float, _f64p]
         L.orc_source_ray.argtypes = [C.POINTER(OrcConfig), C.c_uint64, _f32p, _f32p]
         L.orc_diffuse_dir.argtypes = [_f32p, C.c_uint32, C.c_uint32, _f32p]
         L.orc_philox4x32_10.argtypes = [_u32p, _u32p, _u32p]
@@ -260,6 +263,22 @@ def adjoint(scene: "Scene", cfg: OrcConfig, g, ray_begin: int, ray_end: int, nth
     if rc != 0:
         raise RuntimeError("orc_adjoint failed")
     return sc[0], sc[1], fg, segs.value
+
+
+def fd_pair(scene: "Scene", cfg: OrcConfig, g, ray_begin: int, ray_end: int, h: float, nthreads: int = 0) -> dict:
+    """Central differences with common random numbers at sticking s +- h,
+    decomposed by roulette decisions (orc_fd_pair): every path traced once with
+    weights at s - h, s and s + h on its shared geometry."""
+    gg = np.ascontiguousarray(g, dtype=np.float64)
+    out = np.zeros(8)
+    L = lib()
+    cfg.sticking_field = None
+    if L.orc_fd_pair(scene._h, C.byref(cfg), ray_begin, ray_end, nthreads, _p(gg, _f64p), h, _p(out, _f64p)) != 0:
+        raise RuntimeError("orc_fd_pair failed")
+    two_h = float(np.float32(cfg.sticking + np.float32(h))) - float(np.float32(cfg.sticking - np.float32(h)))
+    return {"fd_all": out[0] / two_h, "fd_unflipped": out[1] / two_h, "held_all": out[2],
+            "held_unflipped": out[3], "paths_flipped": int(out[4]), "decisions_flipped": int(out[5]),
+            "paths_with_roulette": int(out[6]), "L": out[7], "two_h": two_h}
 
 
 def make_config(box_lo, box_hi, *, x_bound=1, y_bound=1, reflection=0, specular_fraction=0.0,

@@ -1051,6 +1051,147 @@ int orc_trace(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, 
   return 0;
 }
 
+/* Central differences with common random numbers, decomposed by roulette
+ * decisions.  Every path is traced once while three weights ride on it: w at
+ * the configured global sticking s, and w+/w- at s + h / s - h.  The path's
+ * geometry (hits, directions) does not depend on s, only on the Russian
+ * roulette decisions (rejection_control.hpp:28-61) that its weights meet, so
+ * all three share it for as long as they are alive; a state that is killed
+ * stops depositing.  At each collision a state's decision is 0 (w >= 0.1, no
+ * roulette), 1 (roulette, survived, w := 0.3) or 2 (roulette, killed).  A path
+ * is "flipped" when the three states do not make the same decisions all the way.
+ * Along the s state the held derivative dL_p/ds is formed exactly as the GPU's
+ * held replay forms it (dv = w + s w', w' -= dv, w' = 0 after a survival).
+ * out[0] = sum over paths of L+ - L-        (divide by 2h: the difference quotient)
+ * out[1] = the same over unflipped paths
+ * out[2] = held dL/ds over all paths
+ * out[3] = held dL/ds over unflipped paths
+ * out[4] = flipped paths
+ * out[5] = collisions at which the +h and -h states, both alive, decide differently
+ * out[6] = paths on which any state met the roulette
+ * out[7] = L at s (sum over paths) */
+static void fd_pair_path(const orc_scene* s, const orc_config* cf, uint64_t id, const double* g, float h,
+                         double* out) {
+  float org[3], dir[3];
+  orc_source_ray(cf, id, org, dir);
+  v3 o = mk(org[0], org[1], org[2]), d = mk(dir[0], dir[1], dir[2]);
+  const float st[3] = {cf->sticking - h, cf->sticking, cf->sticking + h};
+  float w[3] = {1.0f, 1.0f, 1.0f};
+  int alive[3] = {1, 1, 1};
+  double L[3] = {0.0, 0.0, 0.0};
+  double wd = 0.0, held = 0.0;
+  int flipped = 0, met = 0;
+  double flips = 0.0;
+  uint32_t k = 0, nseg = 0;
+  const double lower = cf->roulette_threshold * 1.0f, renew = cf->roulette_weight * 1.0f;
+  while (alive[0] || alive[1] || alive[2]) {
+    if (nseg == cf->max_segments) break;
+    nseg += 1;
+    float th = 0.0f, tb = 0.0f;
+    int32_t p = -1;
+    int hit = closest(s, o, d, cf->tnear, &th, &p);
+    int axis = boundary_exit(cf, o, d, &tb);
+    if (hit && (axis < 0 || th <= tb)) {
+      v3 n = prim_normal(s, p);
+      v3 hp = mk(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
+      if (d.x * n.x + d.y * n.y + d.z * n.z > 0.0f) {
+        o = hp;
+        continue;
+      }
+      double G = g[p];
+      if (p < s->nd && s->nb_ptr)
+        for (int64_t q = s->nb_ptr[p]; q < s->nb_ptr[p + 1]; ++q) {
+          int32_t nb = s->nb_idx[q];
+          if (local_intersect(o, d, disc_c(s, nb), s->dc[4 * nb + 3], disc_n(s, nb))) G += g[nb];
+        }
+      uint32_t u[4];
+      draw4(cf->seed, id, k, cf->job, u);
+      int dec[3] = {-1, -1, -1};
+      for (int j = 0; j < 3; ++j) {
+        if (!alive[j]) continue;
+        const float v = w[j] * st[j];
+        L[j] += G * (double)v;
+        if (j == 1) {
+          const double dv = (double)w[1] + (double)st[1] * wd;
+          held += G * dv;
+          wd -= dv;
+        }
+        w[j] = w[j] - v;
+        if (w[j] == 0.0f) {
+          dec[j] = 3;
+          alive[j] = 0;
+          continue;
+        }
+        dec[j] = 0;
+        if (!((double)w[j] >= lower)) {
+          const double kill = 1.0f - (double)w[j] / renew;
+          met = 1;
+          if ((double)u[0] < kill * 4294967296.0) {
+            dec[j] = 2;
+            alive[j] = 0;
+          } else {
+            dec[j] = 1;
+            w[j] = (float)renew;
+            if (j == 1) wd = 0.0;
+          }
+        }
+      }
+      if (dec[0] != dec[1] || dec[1] != dec[2]) flipped = 1;
+      if (dec[0] >= 0 && dec[2] >= 0 && dec[0] != dec[2]) flips += 1.0;
+      int spec = cf->reflection == 1 ||
+                 (cf->reflection == 2 && (double)u[3] < (double)cf->specular_fraction * 4294967296.0);
+      d = spec ? specular_dir(n, d) : diffuse_dir(n, u[1], u[2]);
+      o = hp;
+      k += 1;
+      continue;
+    }
+    if (axis >= 0) {
+      v3 hp = mk(o.x + d.x * tb, o.y + d.y * tb, o.z + d.z * tb);
+      int periodic = axis == 0 ? cf->x_bound : cf->y_bound;
+      if (periodic) {
+        if (axis == 0) hp.x = d.x > 0.0f ? cf->box_lo[0] : cf->box_hi[0];
+        else hp.y = d.y > 0.0f ? cf->box_lo[1] : cf->box_hi[1];
+      } else {
+        if (axis == 0) d.x = -d.x;
+        else d.y = -d.y;
+      }
+      o = hp;
+      continue;
+    }
+    break;
+  }
+  out[0] += L[2] - L[0];
+  out[2] += held;
+  if (!flipped) {
+    out[1] += L[2] - L[0];
+    out[3] += held;
+  }
+  out[4] += flipped;
+  out[5] += flips;
+  out[6] += met;
+  out[7] += L[1];
+}
+
+int orc_fd_pair(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, int nthreads, const double* g,
+                float h, double* out) {
+  if (cf->sticking_field || cf->window) return 1; /* one global sticking, neighbour deposit */
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  for (int i = 0; i < 8; ++i) out[i] = 0.0;
+#pragma omp parallel num_threads(nthreads)
+  {
+    double o[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = (int64_t)b; i < (int64_t)e; ++i) fd_pair_path(s, cf, (uint64_t)i, g, h, o);
+#pragma omp critical
+    for (int i = 0; i < 8; ++i) out[i] += o[i];
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Neighbourhood: disc_neighborhood.hpp:37-220 restated (divide and conquer  */
 /* on the centre coordinates, strict distance test).                         */

@@ -94,6 +94,13 @@ int orc_trace(const orc_scene* s, const orc_config* cf, uint64_t ray_begin, uint
 int orc_adjoint(const orc_scene* s, const orc_config* cf, uint64_t ray_begin, uint64_t ray_end, int nthreads,
                 const double* g, int unbiased, double* field_grad, double* scalars, uint64_t* segments);
 
+/* Central differences of L = sum_i g_i S1_i at s +- h (global sticking, common
+ * random numbers) for rays [ray_begin, ray_end), split by whether the roulette
+ * decisions of the path differ between s - h, s and s + h; also the held
+ * dL/ds along the path at s.  out[8]: see rtg_oracle.c (fd_pair_path). */
+int orc_fd_pair(const orc_scene* s, const orc_config* cf, uint64_t ray_begin, uint64_t ray_end, int nthreads,
+                const double* g, float h, double* out);
+
 /* One source ray (origin, direction) for ray id; exposes the sampler. */
 void orc_source_ray(const orc_config* cf, uint64_t id, float* org, float* dir);
 /* Diffuse re-emission direction about a normal for two uniforms. */

@@ -847,21 +847,21 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
     if (rc == RTG_OK) rc = prepare_trace(ctx, 0, sample_rays, seed, p);  // the tree changed
     if (rc != RTG_OK) break;
     const size_t first = cand.size();
-    for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT, RTG_SCHED_PLAIN})
+    // the wavefront schedule is not a candidate: its queue traffic lost to the
+    // megakernel on every workload measured (it stays selectable by hand)
+    for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_PLAIN})
       for (int tpb : {64, 128, 256})
         for (int packet : {1, 8, 32})
           for (int stack : {0, 256})
             for (int leaf : {RTG_LEAF_IMMEDIATE, RTG_LEAF_POSTPONED}) {
               if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
-              if (sched == RTG_SCHED_WAVEFRONT && (packet != 1 || tpb == 64 || leaf != RTG_LEAF_IMMEDIATE))
-                continue;  // no refill in a wavefront; its extend kernel tests leaves on the spot
               if (stack == 256 && stack_for(0, ctx->g.depth) == 256) continue;
               if (leaf == RTG_LEAF_POSTPONED && packet == 32) continue;
               cand.push_back(Cand{builder, rtg_launch_config{tpb, packet, stack, sched, leaf}, 0.0f});
             }
     float ms = 0.0f;
     for (size_t i = first; i < cand.size() && rc == RTG_OK; ++i) {
-      rc = run(cand[i].lc, ms);  // warm-up (and, for the wavefront, its queue allocation)
+      rc = run(cand[i].lc, ms);  // warm-up
       if (rc == RTG_OK) rc = run(cand[i].lc, cand[i].ms);
     }
     // the three fastest of this tree again, keep each one's best time

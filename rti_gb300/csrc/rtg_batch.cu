@@ -402,13 +402,13 @@ int rtg_batch_autotune(rtg_batch* b, double fraction, rtg_launch_config* best, d
     return RTG_OK;
   };
   std::vector<rtg_launch_config> cand;
-  for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_WAVEFRONT, RTG_SCHED_PLAIN})
+  // no wavefront candidates (see rtg_autotune)
+  for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_PLAIN})
     for (int tpb : {64, 128, 256})
       for (int packet : {1, 8, 32})
         for (int stack : {0, 256})
           for (int leaf : {RTG_LEAF_IMMEDIATE, RTG_LEAF_POSTPONED}) {
             if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
-            if (sched == RTG_SCHED_WAVEFRONT && (packet != 1 || tpb == 64 || leaf != RTG_LEAF_IMMEDIATE)) continue;
             if (stack == 256 && stack_for(0, b->depth) == 256) continue;
             if (leaf == RTG_LEAF_POSTPONED && packet == 32) continue;
             cand.push_back(rtg_launch_config{tpb, packet, stack, sched, leaf});

@@ -18,6 +18,18 @@
 // written earlier in the same call, so nothing needs clearing, but two calls
 // whose kernels overlap on the GPU (different streams, no ordering) race on
 // it and must be serialised by the caller.
+//
+// Ordering: the kernels are enqueued on the caller's stream after a wait on
+// the event the last trace recorded at its end, so the estimates never read
+// accumulators or areas that the trace is still writing, whichever stream it
+// ran on; the host does not block.
+//
+// The device address of the array is looked up with cudaGetSymbolAddress the
+// first time a CUDA context calls in (the first call on each device, and the
+// first call again after that device's context was destroyed and created
+// anew, e.g. by cudaDeviceReset); that first call should come before any
+// stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -36,20 +48,60 @@ __device__ __align__(256) double g_na_scratch[kNaSlots];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_na_mutex;
-double* g_na_addr[kMaxDevices] = {};
+// per device: the address of the array in the context it was looked up in
+struct NaAddr {
+  unsigned long long ctx_id = 0;
+  double* addr = nullptr;
+};
+NaAddr g_na_addr[kMaxDevices];
 
-// Device address of the scratch array on `device` (the current device),
-// looked up once per device.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Process-unique id of the current CUDA context (0 if the driver cannot say);
+// called with g_na_mutex held:
+// a context created after cudaDeviceReset gets a new id, even where its
+// handle value repeats.  The driver functions are found through the runtime,
+// so the library needs no link against the driver library.
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+    cudaGetLastError();
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of the scratch array on `device` (the current device), set
+// up once per device and context.  Without a context id (a driver that cannot
+// report one) the address is looked up on every call.
 int scratch_address(rtg_context* ctx, int device, double** out) {
   if (device < 0 || device >= kMaxDevices) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "device index too large");
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_addr[device]) {
+  const unsigned long long cid = current_context_id();
+  NaAddr& a = g_na_addr[device];
+  if (cid == 0 || a.ctx_id != cid || !a.addr) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
     if (e != cudaSuccess) return check_cuda(ctx, e, "cudaGetSymbolAddress(no-alloc scratch)");
-    g_na_addr[device] = static_cast<double*>(p);
+    a.addr = static_cast<double*>(p);
+    a.ctx_id = cid;
   }
-  *out = g_na_addr[device];
+  *out = a.addr;
   return RTG_OK;
 }
 
@@ -133,6 +185,8 @@ extern "C" RTG_API int rtg_get_mc_estimates_noalloc(rtg_context* ctx, float* d_o
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   const int64_t nblocks = (np + kNaThreads - 1) / kNaThreads;
   const Geometry& g = ctx->g;
+  // after the trace's last kernel, on whichever stream the trace ran
+  RTG_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev1, 0));
   na_smooth_kernel<<<(unsigned)nblocks, kNaThreads, 0, st>>>(ctx->acc.p, ctx->areas.p, np, g.nd,
                                                             g.nd > 0 ? g.nb_ptr.p : nullptr, g.nb_idx.p, d_out,
                                                             scratch);

@@ -14,9 +14,10 @@ Plug-ins map as follows:
   examples use a constant, main/dev.cpp:214-228);
 * reflection: ``Diffuse()`` (reflection/diffuse.hpp), ``Specular()``
   (reflection/specular.hpp) or ``Mixed(p)``;
-* direction: ``set(PowerCosineDirectionZ(n))`` selects a cos^n source.  In the
-  reference ``device::set`` assigns through a reference member and leaves the
-  cosine source in place (device.hpp:77-80, 295-296); here it takes effect.
+* direction: ``set(direction)`` changes nothing, as in the reference, where
+  ``device::set`` assigns through a reference member bound to the cosine source
+  and copies only the empty ``i_direction`` base (device.hpp:77-80, 295-296);
+  ``set_source_exponent(n)`` (no counterpart there) selects a cos^n source.
 """
 from __future__ import annotations
 
@@ -92,7 +93,7 @@ class Device:
         self.numofrays = 1024                      # device.hpp:289
         self.x_cond = BoundCondition.REFLECTIVE    # device.hpp:292
         self.y_cond = BoundCondition.REFLECTIVE    # device.hpp:293
-        self.direction = CosineDirectionZ()
+        self.source_exponent = 1.0               # cosine_direction_z, device.hpp:295
         self.seed = 0
         self.mcestimates = np.zeros(0, dtype=np.float32)
         self.hitcnts = np.zeros(0, dtype=np.uint64)
@@ -117,7 +118,12 @@ class Device:
         self.y_cond = BoundCondition(cond)
 
     def set(self, direction):
-        self.direction = direction
+        """rti's ``device::set``: the source stays cosine (device.hpp:77-80)."""
+        del direction
+
+    def set_source_exponent(self, n: float):
+        """Extension: a cos^n source (power_cosine_direction_z), n >= 0."""
+        self.source_exponent = float(n)
 
     def set_seed(self, seed: int):
         self.seed = int(seed)
@@ -145,7 +151,7 @@ class Device:
         cfg.reflection = self.reflection.mode
         cfg.specular_fraction = getattr(self.reflection, "specular_fraction", 0.0)
         cfg.sticking = s
-        cfg.source_exponent = getattr(self.direction, "exponent", 1.0)
+        cfg.source_exponent = self.source_exponent
         e.configure(**{k: getattr(cfg, k) for k in ("x_bound", "y_bound", "reflection", "specular_fraction",
                                                     "sticking", "source_exponent")})
         e.set_sticking_field(field)

@@ -43,11 +43,42 @@ def device_accumulators(engine):
     return acc, cnt
 
 
-def allreduce_results(acc, cnt, tally: dict | None = None, group=None):
-    """Sums accumulators, counts and integer tallies over all ranks in place."""
+FIXED_SCALE = 4294967296.0  # RTG_ACCUM_FIXED: S1 holds integer multiples of 2^-32
+
+
+def s1_to_fixed(s1):
+    """The int64 multiples of 2^-32 behind an RTG_ACCUM_FIXED S1 (a float64
+    tensor).  Exact while |S1| < 2^21 on every primitive (the integer fits the
+    53-bit mantissa of the double that carries it)."""
+    import torch
+    return torch.round(s1 * FIXED_SCALE).to(torch.int64)
+
+
+def s1_from_fixed(q):
+    """float64 S1 from int64 multiples of 2^-32, rounded as the library
+    rounds them at the end of a trace: (double)q * 2^-32."""
+    import torch
+    return q.to(torch.float64) * (1.0 / FIXED_SCALE)
+
+
+def allreduce_results(acc, cnt, tally: dict | None = None, group=None, fixed_s1: bool = False):
+    """Sums accumulators, counts and integer tallies over all ranks in place.
+
+    fixed_s1: the ranks traced with RTG_ACCUM_FIXED; S1 (the first n entries
+    of acc) is then summed as int64 multiples of 2^-32, so the sum does not
+    depend on the order of the ranks and equals, bit for bit, one rank that
+    traced every ray (while every rank's |S1| < 2^21 per primitive).  S2..S4
+    are FP64 sums either way."""
     import torch
     import torch.distributed as dist
-    dist.all_reduce(acc, group=group)
+    if fixed_s1:
+        n = cnt.numel()
+        q = s1_to_fixed(acc[:n])
+        dist.all_reduce(q, group=group)
+        dist.all_reduce(acc[n:], group=group)
+        acc[:n] = s1_from_fixed(q)
+    else:
+        dist.all_reduce(acc, group=group)
     dist.all_reduce(cnt, group=group)
     if tally is not None:
         keys = sorted(tally)

@@ -1,8 +1,8 @@
 """Writes the golden fixtures under tests/golden/ from the reference's own tests and data.
 
-Run once in a container where the rti sources are mounted (default
-/root/reference); the fixtures it writes are committed and travel with the
-repository.
+Run once where the rti sources are checked out, with their root as the one
+required argument (``python tests/golden/make_golden.py <rti-root>``); the
+fixtures it writes are committed and travel with the repository.
 
 * area_inside_cases.json -- the 37 known-answer cases of
   test/rti/geo/disc_bounding_box_intersector.cpp, with the expected value
@@ -24,7 +24,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = ""  # the rti source root, from the command line (main)
 TEST = "test/rti/geo/disc_bounding_box_intersector.cpp"
 
 f32 = np.float32
@@ -128,6 +128,10 @@ def normalize_f32(v):
 
 
 def main():
+    global REF
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_golden.py <rti source root>")
+    REF = sys.argv[1]
     src = os.path.join(REF, TEST)
     if not os.path.exists(src):
         raise SystemExit(f"reference tests not found under {REF}")

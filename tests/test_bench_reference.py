@@ -18,7 +18,9 @@ def test_reference_arm_json_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["metric"] == "traced rays/s" and d["unit"] == "rays/s"
     assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1
-    assert d["config"]["workload"] == "hole_triangles" and d["config"]["n_rays_per_step"] == 20000
+    # the GPU arm's configuration; the CPU times a sample of each step's rays
+    assert d["config"]["workload"] == "hole_triangles" and d["config"]["n_rays_per_step"] == 10_000_000
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert cb["sample_rays_per_step"] == 20000
     assert d["e2e"] == {"value": d["value"], "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

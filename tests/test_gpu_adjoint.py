@@ -8,6 +8,8 @@
   of the held estimator (h = 1e-3 relative) within 1e-3 relative;
 * the torch.autograd.Function returns the same numbers as the C ABI.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -112,6 +114,53 @@ def test_global_sticking_gradient_vs_crn_differences(eng):
     fd = (4 * d1 - d2) / 3
     print(f"dL/ds adjoint {ds:.6g}  central differences {d1:.6g} (0.1 s), {d2:.6g} (0.2 s) -> {fd:.6g}")
     assert _rel(ds, fd) < 0.02
+
+
+def test_roulette_flips_at_a_relative_step_of_1e3(eng, oracle_lib):
+    """Why the sticking gradient is not checked against h = 1e-3 s differences.
+
+    Hole of the bench workload at 1e7 rays, s = 0.01, L = bottom-quarter flux.
+    The oracle traces every path once with weights at s - h, s and s + h
+    (h = 1e-3 s) on its shared geometry and counts the Russian-roulette
+    decisions that differ (rejection_control.hpp:44-57).  Every path starts at
+    w = 1 and loses a factor (1 - s) per deposit, so the first roulette comes at
+    the same collision on every path, ceil(ln 0.1 / ln(1 - s)): 229 at s + h,
+    230 at s - h.  The step therefore moves the roulette of every path that
+    reaches it, and the difference quotient over all paths is far from the
+    derivative with the decisions held.  Over the paths with no flipped
+    decision the quotient equals the held derivative (bar 2 %), and the held
+    derivative over all paths equals the GPU's held replay (FP64 order); the
+    GPU's own +-h traces give the oracle's quotient."""
+    h_ = scenes.hole_triangles()
+    eng.upload_triangles(h_.vertices, h_.indices)
+    s0, n = 0.01, 10_000_000
+    eng.configure(box=(h_.box_lo, h_.box_hi), sticking=s0, reflection=2, specular_fraction=0.1, x_bound=1,
+                  y_bound=1, reset=True)
+    g = _bottom_quarter_weights(h_)
+    held_gpu, _, _ = eng.adjoint(g, n, seed=11, unbiased=False)
+    sc = oracle_lib.Scene(tri_vertices=h_.vertices, tri_indices=h_.indices)
+    cfg = oracle_lib.make_config(h_.box_lo, h_.box_hi, sticking=s0, reflection=2, specular_fraction=0.1, seed=11)
+    hh = float(np.float32(1e-3) * np.float32(s0))
+    r = oracle_lib.fd_pair(sc, cfg, g, 0, n, hh)
+    print(f"h = 1e-3 s: {r['decisions_flipped']} roulette decisions flipped on {r['paths_flipped']} paths "
+          f"({r['paths_with_roulette']} paths meet the roulette, {n} rays); difference quotient "
+          f"{r['fd_all']:.6g} over all paths, held derivative {r['held_all']:.6g}; over the unflipped paths "
+          f"{r['fd_unflipped']:.6g} vs {r['held_unflipped']:.6g}")
+    k_plus = math.ceil(math.log(0.1) / math.log(1.0 - (s0 + hh)))
+    k_minus = math.ceil(math.log(0.1) / math.log(1.0 - (s0 - hh)))
+    assert k_plus != k_minus and r["paths_flipped"] == r["paths_with_roulette"] > 0
+    assert _rel(r["fd_unflipped"], r["held_unflipped"]) < 0.02
+    assert _rel(r["held_all"], held_gpu) < 1e-9
+    assert _rel(r["fd_all"], r["held_all"]) > 0.2  # the flips dominate the plain quotient
+
+    def L(s):
+        eng.configure(sticking=s)
+        eng.trace(n, 11)
+        return float(g @ eng.values())
+
+    fd_gpu = (L(float(np.float32(s0) + np.float32(hh))) - L(float(np.float32(s0) - np.float32(hh)))) / r["two_h"]
+    eng.configure(sticking=s0)
+    assert _rel(fd_gpu, r["fd_all"]) < 1e-4
 
 
 def test_exponent_gradient_vs_crn_differences(eng):

@@ -6,7 +6,10 @@ rti's users do (set_points / set_normals / set_grid_spacing / set_x / set_y /
 set_number_of_rays / run / get_mc_estimates / get_hit_cnts), for a particle
 whose sticking comes from get_sticking_probability(), one with a constant
 `rtg_sticking`, one with get_sticking_field(), and the constant one with the
-multi-hit window deposit (set_multi_hit_window)."""
+multi-hit window deposit (set_multi_hit_window).  Every run also calls
+set(power_cosine_direction_z(5)), which must leave the cosine source in place as
+in the reference; the extension set_source_exponent(5) selects cos^5.  The
+Python mirror (rti_gb300.device) is held to the same rule."""
 import os
 import subprocess
 
@@ -48,7 +51,7 @@ std::vector<T> load(const std::string& path, size_t n) {
 }
 
 template <typename P, typename R>
-void run(const std::string& dir, const std::string& tag, size_t n, bool window = false) {
+void run(const std::string& dir, const std::string& tag, size_t n, bool window = false, float exponent = 0) {
   auto pts = load<std::array<float, 3>>(dir + "/points.bin", n);
   auto nrm = load<std::array<float, 3>>(dir + "/normals.bin", n);
   auto rad = load<float>(dir + "/radii.bin", n);
@@ -60,6 +63,10 @@ void run(const std::string& dir, const std::string& tag, size_t n, bool window =
   d.set_y(rti::geo::bound_condition::PERIODIC);
   d.set_number_of_rays(200000);
   if (window) d.set_multi_hit_window(5.0f);
+  // rti's set() leaves the cosine source in place: the flux must not change
+  rti::ray::power_cosine_direction_z<float> cos5(5.0f);
+  d.set(cos5);
+  if (exponent > 0) d.set_source_exponent(exponent);
   d.run();
   auto est = d.get_mc_estimates();
   auto cnt = d.get_hit_cnts();
@@ -81,6 +88,7 @@ int main(int argc, char** argv) {
   run<constant, rti::reflection::mixed<float, 10>>(dir, "constant", n);
   run<field, rti::reflection::specular<float>>(dir, "field", n);
   run<constant, rti::reflection::diffuse<float>>(dir, "window", n, true);
+  run<constant, rti::reflection::diffuse<float>>(dir, "cos5", n, false, 5.0f);
   std::printf("ok\n");
   return 0;
 }
@@ -105,8 +113,9 @@ def test_cpp_dropin_matches_binding(rtg_lib, tmp_path):
     r = subprocess.run([str(exe), str(tmp_path), str(n)], capture_output=True, text=True)
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr
 
-    def expect(sticking_field, reflection, specular_fraction, sticking=0.1):
+    def expect(sticking_field, reflection, specular_fraction, sticking=0.1, exponent=1.0):
         c = L.default_config()
+        c.source_exponent = exponent
         c.x_bound = c.y_bound = L.RTG_BOUND_PERIODIC
         c.reflection = reflection
         c.specular_fraction = specular_fraction
@@ -129,7 +138,8 @@ def test_cpp_dropin_matches_binding(rtg_lib, tmp_path):
     cases = {"per_disc": expect(np.where(ids % 2 == 1, 0.1, 0.3).astype(np.float32), L.RTG_REFLECT_DIFFUSE, 0.0),
              "constant": expect(None, L.RTG_REFLECT_MIXED, np.float32(0.1)),
              "field": expect(np.full(n, 0.25, np.float32), L.RTG_REFLECT_SPECULAR, 1.0),
-             "window": expect_window()}
+             "window": expect_window(),
+             "cos5": expect(None, L.RTG_REFLECT_DIFFUSE, 0.0, exponent=5.0)}
     for tag, (est, cnt) in cases.items():
         est_cpp = np.fromfile(tmp_path / f"{tag}_est.bin", dtype=np.float32)
         cnt_cpp = np.fromfile(tmp_path / f"{tag}_cnt.bin", dtype=np.uint64)
@@ -137,3 +147,25 @@ def test_cpp_dropin_matches_binding(rtg_lib, tmp_path):
         assert np.array_equal(cnt_cpp, cnt), tag
         np.testing.assert_allclose(est_cpp, est, rtol=1e-6, atol=0, err_msg=tag)
         assert cnt_cpp.sum() > 0 and val_cpp.sum() > 0
+
+
+def test_python_mirror_set_direction_keeps_cosine(rtg_lib):
+    from rti_gb300 import device as D
+    t = scenes.trench_discs(domain=1.2, width=0.4, depth=1.0)
+
+    def run(setup):
+        d = D.Device(D.ConstantSticking(0.1))
+        d.set_points(t.points)
+        d.set_normals(t.normals)
+        d.set_grid_spacing(t.radii)
+        d.set_x(D.BoundCondition.PERIODIC)
+        d.set_y(D.BoundCondition.PERIODIC)
+        d.set_number_of_rays(100000)
+        setup(d)
+        d.run()
+        return d.get_hit_cnts()
+
+    base = run(lambda d: None)
+    assert np.array_equal(run(lambda d: d.set(D.PowerCosineDirectionZ(5.0))), base)
+    cos5 = run(lambda d: d.set_source_exponent(5.0))
+    assert not np.array_equal(cos5, base)

@@ -116,6 +116,7 @@ def test_autotune_picks_a_valid_config_and_results_stay(eng):
     cfg, rate = eng.autotune(80000, seed=1)
     assert rate > 0
     assert cfg["threads_per_block"] in (64, 128, 256) and 1 <= cfg["packet"] <= 32
+    assert cfg["scheduling"] != WF  # the wavefront is no autotune candidate
     assert eng.launch_config().as_dict() == cfg and eng.tree_builder in (0, 1)
     _same(ref, _run(eng, 80000, 1))
     eng.set_launch_config()
@@ -153,7 +154,7 @@ def test_batch_wavefront_and_autotune(rtg_lib):
                 assert np.array_equal(r[1], ref[j][1])
                 np.testing.assert_allclose(r[0], ref[j][0], rtol=S1_RTOL, atol=0)
         cfg, rate = b.autotune(0.25)
-        assert rate > 0 and b.launch_config() == cfg
+        assert rate > 0 and b.launch_config() == cfg and cfg["scheduling"] != WF
         b.run(use_graph=True)
         b.synchronize()
         for j in range(len(b)):

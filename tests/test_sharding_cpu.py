@@ -1,6 +1,8 @@
-"""Multi-rank path on CPU: two gloo ranks trace disjoint ray ranges with the
-oracle and sum their accumulators; the result equals one rank tracing every
-ray (counts and tallies bit for bit, S1..S4 to the FP64 summation order)."""
+"""Multi-rank path on CPU: gloo ranks trace disjoint ray ranges with the
+oracle and sum their accumulators with rti_gb300.sharding; the result equals
+one rank tracing every ray (counts and tallies bit for bit, S1..S4 to the FP64
+summation order; with fixed-point S1 accumulation, S1 bit for bit too, for 2
+and 3 ranks with uneven splits)."""
 import os
 
 import numpy as np
@@ -102,3 +104,57 @@ def test_two_gloo_ranks_adjoint_equals_one_rank(tmp_path, oracle_lib):
     sc = np.load(tmp_path / "sc.npy")
     np.testing.assert_allclose(sc, [ds, dn], rtol=1e-10)
     np.testing.assert_allclose(np.load(tmp_path / "fg.npy"), fg, rtol=1e-10, atol=1e-12 * np.abs(fg).max())
+
+
+# uneven ray ranges: (world, boundaries)
+FIXED_SPLITS = {2: [0, 1234, 7001], 3: [0, 100, 5000, 7001]}
+
+
+def _fixed_worker(rank, world, port, out_dir):
+    from oracle import oracle as O
+    from rti_gb300 import scenes
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    t = scenes.trench_discs(domain=0.6, width=0.2, depth=0.4)
+    s = O.Scene(t.xyzr, t.normals)
+    s.neighbors()
+    cfg = O.make_config(t.box_lo, t.box_hi, sticking=0.2, seed=9, accum_fixed=1)
+    cuts = FIXED_SPLITS[world]
+    r = s.trace(cfg, cuts[rank], cuts[rank + 1], nthreads=1)
+    acc = torch.from_numpy(stack_accumulators(r.s1, r.s2, r.s3, r.s4))
+    cnt = torch.from_numpy(r.counts.astype(np.int64))
+    allreduce_results(acc, cnt, fixed_s1=True)
+    if rank == 0:
+        np.save(os.path.join(out_dir, f"acc{world}.npy"), acc.numpy())
+        np.save(os.path.join(out_dir, f"cnt{world}.npy"), cnt.numpy())
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_fixed_point_sharded_sum_is_bit_identical(tmp_path, oracle_lib, world):
+    """RTG_ACCUM_FIXED: S1 of every rank is an integer multiple of 2^-32 and
+    allreduce_results(fixed_s1=True) sums the integers, so the sharded S1 equals
+    one rank's S1 bit for bit whatever the split."""
+    import socket
+    from oracle import oracle as O
+    from rti_gb300 import scenes
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    mp.start_processes(_fixed_worker, args=(world, port, str(tmp_path)), nprocs=world, join=True,
+                       start_method="spawn")
+    t = scenes.trench_discs(domain=0.6, width=0.2, depth=0.4)
+    s = O.Scene(t.xyzr, t.normals)
+    s.neighbors()
+    ref = s.trace(O.make_config(t.box_lo, t.box_hi, sticking=0.2, seed=9, accum_fixed=1), 0, 7001, nthreads=1)
+    acc = np.load(tmp_path / f"acc{world}.npy")
+    n = len(ref.s1)
+    assert np.array_equal(acc[:n], ref.s1)  # bit for bit
+    assert np.array_equal(np.load(tmp_path / f"cnt{world}.npy"), ref.counts.astype(np.int64))
+    np.testing.assert_allclose(acc[n:], np.concatenate([ref.s2, ref.s3, ref.s4]), rtol=1e-12)
+    # the plain FP64 sum of the same per-rank S1 is not guaranteed to be exact;
+    # the integer sum is, by construction
+    from rti_gb300.sharding import s1_from_fixed, s1_to_fixed
+    q = s1_to_fixed(torch.from_numpy(ref.s1))
+    assert torch.equal(s1_from_fixed(q), torch.from_numpy(ref.s1))
