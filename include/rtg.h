@@ -202,6 +202,29 @@ RTG_API int rtg_get_tree_depth(const rtg_context* ctx, int32_t* depth);
 #define RTG_TREE_PLOC 1
 RTG_API int rtg_set_tree_builder(rtg_context* ctx, int32_t builder);
 RTG_API int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder);
+/* Which tree the closest-hit queries traverse (no counterpart in rti; Embree
+ * chooses its own):
+ *   RTG_NODES_BINARY (2): the binary tree itself (64-byte nodes, both child
+ *     boxes in float);
+ *   RTG_NODES_WIDE (8): a compressed 8-wide tree collapsed from it after every
+ *     build and refit (96-byte nodes, child boxes as bytes on a per-node
+ *     power-of-two grid, children ordered by direction).  Its boxes contain
+ *     the binary boxes, so results are the same bit for bit;
+ *   RTG_NODES_AUTO (0, the default): wide when the binary nodes and the
+ *     primitive records outgrow the L2 cache, else binary.  Measured: the wide
+ *     tree moves a third less DRAM traffic and traces a 4.19 M-disc surface
+ *     13-16 % faster, but costs more instructions per query and traces
+ *     L2-resident surfaces (200 k triangles, 98 k discs) 3-10 % slower.
+ * A scene with a node wider than 4080 units, or a wide tree whose traversal
+ * stack would exceed 256 entries, is traced over the binary tree whatever this
+ * says.  The postponed leaf tests (RTG_LEAF_POSTPONED) and the multi-hit
+ * window's interval queries always use the binary tree.  rtg_autotune tries
+ * both for its fastest candidates. */
+#define RTG_NODES_AUTO 0
+#define RTG_NODES_BINARY 2
+#define RTG_NODES_WIDE 8
+RTG_API int rtg_set_node_width(rtg_context* ctx, int32_t width);
+RTG_API int rtg_get_node_width(const rtg_context* ctx, int32_t* width);
 /* What a front-face disc hit deposits.  rti has two treatments of
  * overlapping discs:
  *   RTG_DEPOSIT_NEIGHBORS (default): w*s on the hit disc and on every
@@ -252,10 +275,12 @@ RTG_API int rtg_inject_alloc_failure(rtg_context* ctx, int64_t after);
  * or plain; the wavefront schedule, slower on every workload measured, is
  * left to rtg_set_launch_config) on source
  * rays [0, sample_rays) with `seed` under the current surface and
- * configuration; keeps the fastest pair as the context's tree and launch
- * configuration and returns the latter (best and best_rays_per_s may be NULL;
- * rtg_get_tree_builder tells the tree).  Leaves no trace results behind
- * (trace again afterwards). */
+ * configuration, over the node width RTG_NODES_AUTO picks; re-times the three
+ * fastest of each tree with their stacks in the other memory and over the
+ * other node width; keeps the fastest as the context's tree, node width and
+ * launch configuration and returns the latter (best and best_rays_per_s may
+ * be NULL; rtg_get_tree_builder and rtg_get_node_width tell the rest).  Leaves
+ * no trace results behind (trace again afterwards). */
 RTG_API int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
                          double* best_rays_per_s);
 

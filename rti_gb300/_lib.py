@@ -45,7 +45,8 @@ EXPORTS = [
     "rtg_batch_autotune", "rtg_write_vtp", "rtg_write_vtp_discs", "rtg_write_vtp_triangles", "rtg_write_vtp_mixed",
     "rtg_read_point_cloud", "rtg_read_triangles", "rtg_set_tree_builder", "rtg_get_tree_builder",
     "rtg_set_deposit_mode", "rtg_get_deposit_mode", "rtg_set_accumulation", "rtg_get_accumulation",
-    "rtg_set_visit_limit", "rtg_get_visit_limit", "rtg_inject_alloc_failure",
+    "rtg_set_visit_limit", "rtg_get_visit_limit", "rtg_inject_alloc_failure", "rtg_set_node_width",
+    "rtg_get_node_width",
 ]
 
 RTG_ADJ_HELD = 0
@@ -64,6 +65,9 @@ RTG_ACCUM_FP64 = 0
 RTG_ACCUM_FIXED = 1
 RTG_DEPOSIT_NEIGHBORS = 0
 RTG_DEPOSIT_WINDOW = 1
+RTG_NODES_AUTO = 0
+RTG_NODES_BINARY = 2
+RTG_NODES_WIDE = 8
 
 
 class RtgConfig(C.Structure):
@@ -199,6 +203,8 @@ def load(path: str | None = None):
         "rtg_read_triangles": (C.c_int, [C.c_char_p, _i64p, _f32p, _i64p, _u32p, C.c_char_p, C.c_int32]),
         "rtg_set_tree_builder": (C.c_int, [_ctx, C.c_int32]),
         "rtg_get_tree_builder": (C.c_int, [_ctx, _i32p]),
+        "rtg_set_node_width": (C.c_int, [_ctx, C.c_int32]),
+        "rtg_get_node_width": (C.c_int, [_ctx, _i32p]),
         "rtg_set_deposit_mode": (C.c_int, [_ctx, C.c_int32, C.c_float]),
         "rtg_get_deposit_mode": (C.c_int, [_ctx, _i32p, _f32p]),
         "rtg_set_visit_limit": (C.c_int, [_ctx, C.c_uint64]),

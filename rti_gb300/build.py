@@ -21,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librtg.so")
 LIB_CHECKED = os.path.join(HERE, "librtg_checked.so")  # -DRTG_CHECKED: device bounds checks (tests)
 SOURCES = ["rtg_api.cu", "rtg_batch.cu", "rtg_lbvh.cu", "rtg_noalloc.cu", "rtg_sort.cu", "rtg_surface.cu", "rtg_trace.cu",
-           "rtg_trace_batched.cu", "rtg_vtk.cpp", "rtg_wavefront.cu"]
+           "rtg_trace_batched.cu", "rtg_vtk.cpp", "rtg_wavefront.cu", "rtg_wide.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "-I", os.path.join(ROOT, "include")]

@@ -366,6 +366,10 @@ void drop_surface(rtg_context* ctx) {
   dfree(g.disc); dfree(g.tri); dfree(g.nodes);
   dfree(g.leaf_ref); dfree(g.leaf_prim); dfree(g.parent); dfree(g.prim_lo); dfree(g.prim_hi);
   dfree(g.refit_flags); dfree(g.nb_ptr); dfree(g.nb_idx); dfree(g.nb_slot); dfree(g.disc_slot);
+  dfree(g.wnodes);
+  dfree(g.wnodes);
+  g.n_wnodes = 0;
+  g.wide_stack = 0;
   dfree(ctx->sticking_field);
   g.nd = g.nt = g.nv = 0;
   g.nb_nnz = 0;
@@ -762,6 +766,21 @@ int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder) {
   return RTG_OK;
 }
 
+int rtg_set_node_width(rtg_context* ctx, int32_t width) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (width != RTG_NODES_AUTO && width != RTG_NODES_BINARY && width != RTG_NODES_WIDE)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "node width must be RTG_NODES_AUTO, _BINARY or _WIDE");
+  if (width != ctx->node_width) ++ctx->version;  // batch jobs hold scene views
+  ctx->node_width = width;
+  return RTG_OK;
+}
+
+int rtg_get_node_width(const rtg_context* ctx, int32_t* width) {
+  if (!ctx || !width) return RTG_ERR_INVALID_ARGUMENT;
+  *width = ctx->node_width;
+  return RTG_OK;
+}
+
 int rtg_set_deposit_mode(rtg_context* ctx, int32_t mode, float window_factor) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   if (mode != RTG_DEPOSIT_NEIGHBORS && mode != RTG_DEPOSIT_WINDOW)
@@ -822,8 +841,17 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
   cudaStream_t st = ctx->stream;
   const rtg_launch_config keep = ctx->lc;
   const int32_t keep_builder = ctx->g.builder;
-  auto run = [&](const rtg_launch_config& lc, float& ms) -> int {
-    ctx->lc = lc;
+  const int32_t keep_width = ctx->node_width;
+  struct Cand {
+    int32_t builder;
+    int32_t width;  // RTG_NODES_BINARY or RTG_NODES_WIDE
+    rtg_launch_config lc;
+    float ms;
+  };
+  auto run = [&](const Cand& c, float& ms) -> int {
+    ctx->lc = c.lc;
+    ctx->node_width = c.width;
+    p.s = scene_view(ctx);
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * np * sizeof(double), st));
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->cnt.p, 0, np * sizeof(unsigned long long), st));
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
@@ -834,11 +862,6 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
     RTG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->evk0, ctx->evk1));
     return RTG_OK;
   };
-  struct Cand {
-    int32_t builder;
-    rtg_launch_config lc;
-    float ms;
-  };
   std::vector<Cand> cand;
   int rc = RTG_OK;
   for (int32_t builder : {RTG_TREE_KARRAS, RTG_TREE_PLOC}) {
@@ -847,6 +870,7 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
     if (rc == RTG_OK) rc = prepare_trace(ctx, 0, sample_rays, seed, p);  // the tree changed
     if (rc != RTG_OK) break;
     const size_t first = cand.size();
+    const int32_t width = outgrows_l2(ctx) ? RTG_NODES_WIDE : RTG_NODES_BINARY;  // the automatic choice
     // the wavefront schedule is not a candidate: its queue traffic lost to the
     // megakernel on every workload measured (it stays selectable by hand)
     for (int sched : {RTG_SCHED_MEGAKERNEL, RTG_SCHED_PLAIN})
@@ -855,14 +879,14 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
           for (int stack : {0, 256})
             for (int leaf : {RTG_LEAF_IMMEDIATE, RTG_LEAF_POSTPONED}) {
               if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
-              if (stack == 256 && stack_for(0, ctx->g.depth) == 256) continue;
+              if (stack == 256 && stack_for(0, traversal_depth(ctx)) == 256) continue;
               if (leaf == RTG_LEAF_POSTPONED && packet == 32) continue;
-              cand.push_back(Cand{builder, rtg_launch_config{tpb, packet, stack, sched, leaf}, 0.0f});
+              cand.push_back(Cand{builder, width, rtg_launch_config{tpb, packet, stack, sched, leaf}, 0.0f});
             }
     float ms = 0.0f;
     for (size_t i = first; i < cand.size() && rc == RTG_OK; ++i) {
-      rc = run(cand[i].lc, ms);  // warm-up
-      if (rc == RTG_OK) rc = run(cand[i].lc, cand[i].ms);
+      rc = run(cand[i], ms);  // warm-up
+      if (rc == RTG_OK) rc = run(cand[i], cand[i].ms);
     }
     // the three fastest of this tree again, keep each one's best time
     std::vector<size_t> order;
@@ -870,7 +894,7 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
     std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cand[a].ms < cand[b].ms; });
     for (size_t r = 0; r < 2 && rc == RTG_OK; ++r)
       for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
-        rc = run(cand[order[q]].lc, ms);
+        rc = run(cand[order[q]], ms);
         if (rc == RTG_OK && ms < cand[order[q]].ms) cand[order[q]].ms = ms;
       }
     // the three fastest with their stacks in the other memory, best of two
@@ -879,18 +903,32 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
       if (alt.lc.scheduling == RTG_SCHED_WAVEFRONT) continue;
       alt.lc.stack_memory = shared_stack(ctx, alt.lc) ? RTG_STACK_LOCAL : RTG_STACK_SHARED;
       float m2 = 0.0f;
-      rc = run(alt.lc, alt.ms);
-      if (rc == RTG_OK) rc = run(alt.lc, m2);
+      rc = run(alt, alt.ms);
+      if (rc == RTG_OK) rc = run(alt, m2);
       if (rc == RTG_OK) {
         alt.ms = std::min(alt.ms, m2);
         cand.push_back(alt);
       }
     }
+    // the three fastest over the other tree layout (binary / wide), best of two
+    if (ctx->g.n_wnodes > 0)
+      for (size_t q = 0; q < order.size() && q < 3 && rc == RTG_OK; ++q) {
+        Cand alt = cand[order[q]];
+        alt.width = alt.width == RTG_NODES_WIDE ? RTG_NODES_BINARY : RTG_NODES_WIDE;
+        float m2 = 0.0f;
+        rc = run(alt, alt.ms);
+        if (rc == RTG_OK) rc = run(alt, m2);
+        if (rc == RTG_OK) {
+          alt.ms = std::min(alt.ms, m2);
+          cand.push_back(alt);
+        }
+      }
   }
   ctx->traced = false;
   ctx->finalized = false;
   if (rc != RTG_OK || cand.empty()) {
     ctx->lc = keep;
+    ctx->node_width = keep_width;
     rtg_set_tree_builder(ctx, keep_builder);
     return rc != RTG_OK ? rc : set_error(ctx, RTG_ERR_INTERNAL, "autotune found no candidate");
   }
@@ -899,6 +937,8 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
     if (cand[i].ms < cand[bi].ms) bi = i;
   RTG_TRY(rtg_set_tree_builder(ctx, cand[bi].builder));
   ctx->lc = cand[bi].lc;
+  ctx->node_width = cand[bi].width;
+  ++ctx->version;
   if (best) *best = cand[bi].lc;
   if (best_rays_per_s) *best_rays_per_s = cand[bi].ms > 0.0f ? sample_rays / (cand[bi].ms * 1e-3) : 0.0;
   return RTG_OK;

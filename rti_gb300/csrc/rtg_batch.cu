@@ -148,7 +148,7 @@ int refresh_jobs(rtg_batch* b) {
   }
   if (changed) {
     b->depth = 0;
-    for (const Job& j : b->jobs) b->depth = std::max(b->depth, j.scene->g.depth);
+    for (const Job& j : b->jobs) b->depth = std::max(b->depth, traversal_depth(j.scene));
     b->tables_ready = false;
     drop_graph(b);
   }
@@ -237,7 +237,7 @@ int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint6
     return rc;
   }
   b->jobs.push_back(j);
-  if (scene->g.depth > b->depth) b->depth = scene->g.depth;
+  if (traversal_depth(scene) > b->depth) b->depth = traversal_depth(scene);
   b->tables_ready = false;
   drop_graph(b);
   if (job_out) *job_out = (int32_t)(b->jobs.size() - 1);

@@ -28,6 +28,27 @@ struct __align__(16) Node {
   uint4 d;
 };
 
+// One node of the compressed 8-wide tree the closest-hit query traverses
+// (collapsed from the binary LBVH after every build and refit; rtg_wide.cu).
+// 96 bytes, read by three 256-bit loads:
+//   w[0..2]  node origin p (float bits), an exact multiple of the axis quantum
+//   w[3]     biased exponents e_x, e_y, e_z of the quanta 2^e (bytes 0..2) and
+//            the leaf mask (byte 3: bit s set when child slot s is a
+//            primitive or empty)
+//   w[4..11] child references by slot (kLeafBit/kTriBit as in Node; an
+//            internal child is a wide-node index; kNoChild = empty slot)
+//   w[12..23] quantised child boxes, one byte per slot: lo.x (w12, w13),
+//            lo.y, lo.z, hi.x, hi.y, hi.z; box = p + q * 2^e, conservative
+//            (floor for lo, ceil for hi); an empty slot has lo = 255, hi = 0.
+// Slot s holds the child that lies most towards the corner whose axis signs
+// are the bits of s (set = +), so a ray whose direction signs form the octant
+// code o visits the slots in the order i ^ o, i = 0..7, nearly front to back.
+struct __align__(32) WideNode {
+  uint32_t w[24];
+};
+constexpr int kWide = 8;
+constexpr uint32_t kNoChild = 0xFFFFFFFFu;
+
 // LBVH topology builders over the Morton-ordered leaves.
 constexpr int32_t kBuilderKarras = 0;  // Karras 2012 radix tree (split at the highest differing key bit)
 constexpr int32_t kBuilderPloc = 1;    // Meister and Bittner 2018 locally-ordered clustering
@@ -49,6 +70,10 @@ struct SceneView {
   int32_t nt;
   const Node* nodes;
   uint32_t root;        // child reference of the root (internal node 0 or a leaf)
+  // the 8-wide compressed tree of the closest-hit query (root = wide node 0),
+  // or nullptr: closest hits traverse the binary nodes
+  const WideNode* wnodes;
+  uint32_t n_wnodes;
   // neighbour CSR: rows by original disc id, columns as disc slots (the
   // neighbour's record in `disc` carries its original id)
   const int64_t* nb_ptr;
@@ -137,6 +162,10 @@ struct Geometry {
   float tri_min[3] = {0, 0, 0}, tri_max[3] = {0, 0, 0};
   int32_t depth = 0;  // internal nodes on the longest root-to-leaf path
   int32_t builder = 0;  // kBuilderKarras or kBuilderPloc
+  // 8-wide compressed tree (rtg_wide.cu)
+  DBuf<WideNode> wnodes;
+  uint32_t n_wnodes = 0;
+  int32_t wide_stack = 0;  // traversal stack entries the wide tree can need
 };
 
 // Wavefront scheduling state (device buffers, lazily allocated).
@@ -178,6 +207,7 @@ struct rtg_context {
   bool finalized = false;
   float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
   rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL, RTG_LEAF_IMMEDIATE};
+  int32_t node_width = 0;  // RTG_NODES_*: closest hits over the binary or the wide tree
   int32_t deposit_mode = RTG_DEPOSIT_NEIGHBORS;
   int32_t accum = RTG_ACCUM_FP64;
   float window_factor = 5.0f;  // point_cloud_context.hpp:163
@@ -210,6 +240,8 @@ int radix_sort_pairs(rtg_context* ctx, uint32_t* d_keys, uint32_t* d_vals, uint3
 // lbvh.cu
 int build_lbvh(rtg_context* ctx);      // full build from the by-id primitive data
 int refit_lbvh(rtg_context* ctx);      // recompute boxes, keep topology
+// wide.cu: the 8-wide compressed tree from the binary one (after a build or refit)
+int build_wide(rtg_context* ctx, cudaStream_t st);
 // surface.cu
 int build_neighbors(rtg_context* ctx);
 int compute_areas(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi);
@@ -222,6 +254,14 @@ int launch_trace(rtg_context* ctx, const TraceParams& p, cudaStream_t st, int mo
 int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim,
                        float* d_t, unsigned long long* d_errors, cudaStream_t st);
 SceneView scene_view(rtg_context* ctx);
+// whether the binary tree and the primitive records of ctx outgrow the L2 cache
+bool outgrows_l2(const rtg_context* ctx);
+// whether closest hits of ctx traverse the wide tree (chosen, built, and its
+// stack need within the largest stack)
+bool use_wide(const rtg_context* ctx);
+// the traversal stack depth a query of ctx can need (binary tree depth, or
+// the wide tree's stack need when it is used)
+int traversal_depth(const rtg_context* ctx);
 // stack entries for a requested depth (0 = automatic) and a tree depth: 32, 64 or 256
 int stack_for(int requested, int tree_depth);
 // RTG_ACCUM_FIXED: s1 between double and int64 multiples of 2^-32, in place

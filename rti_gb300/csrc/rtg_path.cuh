@@ -48,6 +48,19 @@ __device__ __forceinline__ bool leaf_in_range(const SceneView& s, uint32_t ref) 
 }
 constexpr uint32_t kNoLeaf = 0xFFFFFFFFu;  // no child reference: slots stay below kSlotMask
 
+// Maximum and minimum of three floats in one instruction (sm_100+); exact,
+// so the result equals the two-input forms'.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 __device__ __forceinline__ float safe_inv(float d) {
   if (fabsf(d) < 1e-30f) d = d < 0.0f ? -1e-30f : 1e-30f;
   return 1.0f / d;
@@ -63,8 +76,8 @@ __device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, flo
   float t0x = (lx - r.o.x) * r.idr.x, t1x = (hx - r.o.x) * r.idr.x;
   float t0y = (ly - r.o.y) * r.idr.y, t1y = (hy - r.o.y) * r.idr.y;
   float t0z = (lz - r.o.z) * r.idr.z, t1z = (hz - r.o.z) * r.idr.z;
-  tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
-  float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+  tn = max3f(fminf(t0x, t1x), fminf(t0y, t1y), fmaxf(fminf(t0z, t1z), 0.0f));
+  float tf = min3f(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fmaxf(t0z, t1z));
   return tn <= tf * 1.0000005f && tn <= tmax * 1.0000005f + 1e-30f;
 }
 
@@ -108,6 +121,123 @@ __device__ __forceinline__ void test_leaf(const SceneView& s, uint32_t ref, cons
   }
 }
 
+// Child reference of slot c (0..7) from the eight references of a wide node,
+// by selects rather than an indexed (local-memory) array.
+__device__ __forceinline__ uint32_t pick8(const uint32_t* r, uint32_t c) {
+  const bool b0 = c & 1u, b1 = c & 2u, b2 = c & 4u;
+  const uint32_t a01 = b0 ? r[1] : r[0], a23 = b0 ? r[3] : r[2];
+  const uint32_t a45 = b0 ? r[5] : r[4], a67 = b0 ? r[7] : r[6];
+  const uint32_t lo = b1 ? a23 : a01, hi = b1 ? a67 : a45;
+  return b2 ? hi : lo;
+}
+
+// Bit i of the result is bit (i ^ o) of m (an 8-bit mask): the slots of a
+// wide node in the visiting order of a ray with octant code o.
+__device__ __forceinline__ uint32_t xor_perm8(uint32_t m, uint32_t o) {
+  if (o & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+  if (o & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+  if (o & 4u) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+  return m;
+}
+
+// Closest hit over the compressed 8-wide tree (WideNode, rtg_wide.cu).  One
+// node = three 256-bit loads; its eight child boxes are tested with two
+// instructions per slab plane: q as the float 2^23 + q by a byte permute, then
+// t = (2^23 + q) a + c with a = 2^e / d (exact) and c = (p - o) / d - 2^23 a
+// moved outwards by a margin m = 1.02 |a| + 2^-21 |(p - o) / d|, which bounds
+// every rounding on the way (c, the shift, and the final FMA: |t| is at most
+// 255 |a| + |(p - o) / d|), so the interval tested always contains the exact
+// slab interval of the decoded box -- and the decoded box contains the binary
+// tree's box of the same child.  A box the exact test misses holds no
+// primitive hit (the primitive boxes are padded well beyond rounding), and
+// the exact entry distance of a box holding a hit at t <= bt is <= bt, so the
+// test is tn <= min(tf, bt) without a relative slack.  Hit primitives are tested on the spot; the
+// internal children hit are visited in the ray's octant order (xor_perm8),
+// the nearest-first one at once and the others from the stack.  The closest
+// hit (ties to the lower id) is therefore the binary traversal's.
+// lstack: the caller's local stack (SST = 0), else sstk: a shared column.
+template <int STACK, int SST, typename Count>
+__device__ __forceinline__ bool closest_hit_wide(const SceneView& s, const Ray& r, float tnear, float& bt, int& bid,
+                                                 uint32_t& bref, Count& errs, uint32_t* lstack, uint32_t* sstk) {
+  auto stack = [&](int i) -> uint32_t& { return SST ? sstk[i * SST] : lstack[i]; };
+  int sp = 0;
+  const uint32_t oct = (r.idr.x < 0.0f ? 1u : 0u) | (r.idr.y < 0.0f ? 2u : 0u) | (r.idr.z < 0.0f ? 4u : 0u);
+  uint32_t cur = 0;
+  const uint32_t max_iter = s.max_visits;
+  for (uint32_t it = 0;; ++it) {
+    if (it >= max_iter || (kChecked && cur >= s.n_wnodes)) {
+      errs += 1;
+      break;
+    }
+    uint32_t w[24];
+    const uint32_t* np_ = s.wnodes[cur].w;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+          : "=r"(w[8 * k]), "=r"(w[8 * k + 1]), "=r"(w[8 * k + 2]), "=r"(w[8 * k + 3]), "=r"(w[8 * k + 4]),
+            "=r"(w[8 * k + 5]), "=r"(w[8 * k + 6]), "=r"(w[8 * k + 7])
+          : "l"(np_ + 8 * k));
+    float a[3], cn[3], cf[3];
+    uint32_t nw[3][2], fw[3][2];
+    const float oo[3] = {r.o.x, r.o.y, r.o.z}, id[3] = {r.idr.x, r.idr.y, r.idr.z};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      const float sc = __uint_as_float(((w[3] >> (8 * ax)) & 0xFFu) << 23);  // 2^e
+      a[ax] = sc * id[ax];
+      const float b = (__uint_as_float(w[ax]) - oo[ax]) * id[ax];
+      const float c = fmaf(-8388608.0f, a[ax], b);
+      const float m = fmaf(fabsf(b), 0x1p-21f, 1.02f * fabsf(a[ax]));
+      cn[ax] = c - m;
+      cf[ax] = c + m;
+      const bool pos = id[ax] >= 0.0f;  // near plane = lo for a positive direction, else hi
+      nw[ax][0] = pos ? w[12 + 2 * ax] : w[18 + 2 * ax];
+      nw[ax][1] = pos ? w[13 + 2 * ax] : w[19 + 2 * ax];
+      fw[ax][0] = pos ? w[18 + 2 * ax] : w[12 + 2 * ax];
+      fw[ax][1] = pos ? w[19 + 2 * ax] : w[13 + 2 * ax];
+    }
+    uint32_t hit = 0u;
+#pragma unroll
+    for (int c = 0; c < kWide; ++c) {
+      const uint32_t sel = 0x7540u | (uint32_t)(c & 3);  // byte c of the word, then 0x00, 0x00, 0x4B
+      float tn[3], tf[3];
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) {
+        const float qn = __uint_as_float(__byte_perm(nw[ax][c >> 2], 0x4B000000u, sel));
+        const float qf = __uint_as_float(__byte_perm(fw[ax][c >> 2], 0x4B000000u, sel));
+        tn[ax] = fmaf(qn, a[ax], cn[ax]);
+        tf[ax] = fmaf(qf, a[ax], cf[ax]);
+      }
+      if (max3f(tn[0], tn[1], fmaxf(tn[2], 0.0f)) <= min3f(tf[0], tf[1], fminf(tf[2], bt))) hit |= 1u << c;
+    }
+    const uint32_t lm = w[3] >> 24;
+    uint32_t leaves = hit & lm;
+    while (leaves) {
+      const uint32_t c = (uint32_t)__ffs(leaves) - 1u;
+      leaves &= leaves - 1u;
+      const uint32_t lf = pick8(w + 4, c);
+      if (lf == kNoChild) continue;
+      if (!kChecked || leaf_in_range(s, lf)) test_leaf(s, lf, r, tnear, bt, bid, bref);
+      else errs += 1;
+    }
+    uint32_t pm = xor_perm8(hit & ~lm, oct);
+    if (pm) {
+      const uint32_t first = (uint32_t)__ffs(pm) - 1u;
+      pm &= pm - 1u;
+      while (pm) {  // the others farthest first, so that the nearest is on top
+        const uint32_t i = 31u - (uint32_t)__clz(pm);
+        pm ^= 1u << i;
+        if (sp < STACK) stack(sp++) = pick8(w + 4, i ^ oct);
+        else errs += 1;
+      }
+      cur = pick8(w + 4, first ^ oct);
+    } else {
+      if (sp == 0) break;
+      cur = stack(--sp);
+    }
+  }
+  return bid != INT_MAX;
+}
+
 // Closest primitive hit; returns false when nothing is hit.  errs counts
 // stack overflows and iteration-limit trips (both end the query).
 // POSTPONE = false: a leaf child whose box the ray enters is tested on the
@@ -130,6 +260,7 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   bid = INT_MAX;
   bref = 0xFFFFFFFFu;
   uint32_t lstack[SST ? 1 : STACK];
+  if (!POSTPONE && s.wnodes) return closest_hit_wide<STACK, SST>(s, r, tnear, bt, bid, bref, errs, lstack, sstk);
   auto stack = [&](int i) -> uint32_t& { return SST ? sstk[i * SST] : lstack[i]; };
   int sp = 0;
   uint32_t cur = s.root;

@@ -94,14 +94,22 @@ int s1_to_double(rtg_context* ctx, double* s1, int64_t n, cudaStream_t st) {
   return RTG_OK;
 }
 
-bool shared_stack(rtg_context* ctx, const rtg_launch_config& lc) {
-  if (lc.stack_memory == RTG_STACK_SHARED) return true;
-  if (lc.stack_memory == RTG_STACK_LOCAL) return false;
+// Whether the tree and the primitive records of ctx outgrow the L2 cache.
+bool outgrows_l2(const rtg_context* ctx) {
   int l2 = 0;
-  if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
   const Geometry& g = ctx->g;
   const size_t bytes = g.nodes.n * sizeof(Node) + (g.disc.n + g.tri.n) * sizeof(float4);
   return l2 > 0 && bytes > (size_t)l2;
+}
+
+bool shared_stack(rtg_context* ctx, const rtg_launch_config& lc) {
+  if (lc.stack_memory == RTG_STACK_SHARED) return true;
+  if (lc.stack_memory == RTG_STACK_LOCAL) return false;
+  return outgrows_l2(ctx);
 }
 
 int stack_for(int requested, int tree_depth) {
@@ -128,9 +136,22 @@ int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc) {
   return RTG_OK;
 }
 
+bool use_wide(const rtg_context* ctx) {
+  if (ctx->g.n_wnodes == 0 || ctx->g.wide_stack > 256) return false;
+  if (ctx->node_width == RTG_NODES_AUTO) return outgrows_l2(ctx);
+  return ctx->node_width == RTG_NODES_WIDE;
+}
+
+int traversal_depth(const rtg_context* ctx) {
+  return use_wide(ctx) ? std::max(ctx->g.depth, ctx->g.wide_stack) : ctx->g.depth;
+}
+
 SceneView scene_view(rtg_context* ctx) {
   const Geometry& g = ctx->g;
   SceneView s{};
+  const bool wide = use_wide(ctx);
+  s.wnodes = wide ? g.wnodes.p : nullptr;
+  s.n_wnodes = wide ? g.n_wnodes : 0u;
   s.disc = g.disc.p;
   s.nd = (int32_t)g.nd;
   s.tri = g.tri.p;
@@ -148,7 +169,7 @@ SceneView scene_view(rtg_context* ctx) {
 
 int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int mode) {
   const rtg_launch_config& lc = ctx->lc;
-  const int stack = stack_for(lc.stack_depth, ctx->g.depth);
+  const int stack = stack_for(lc.stack_depth, traversal_depth(ctx));
   TraceParams p = p_in;
   p.packet = lc.packet;
   const uint64_t nrays = p.ray_end - p.ray_begin;
@@ -163,7 +184,7 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
     RTG_CUDA(ctx, cudaMemcpyAsync(wf.one_job.p, &p, sizeof p, cudaMemcpyHostToDevice, st));
     RTG_CUDA(ctx, cudaMemcpyAsync(wf.one_prefix.p, pre, sizeof pre, cudaMemcpyHostToDevice, st));
     RTG_CUDA(ctx, cudaStreamSynchronize(st));  // the host copies above are locals
-    return launch_wavefront(ctx, p, wf.one_job.p, wf.one_prefix.p, 1, nrays, st, lc, ctx->g.depth);
+    return launch_wavefront(ctx, p, wf.one_job.p, wf.one_prefix.p, 1, nrays, st, lc, traversal_depth(ctx));
   }
   int tpb = 128, sms = 0, per_sm = 0;
   PathKernel kern = pick_kernel(mode, lc.threads_per_block, stack, lc.leaf_tests == RTG_LEAF_POSTPONED,

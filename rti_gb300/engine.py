@@ -186,6 +186,17 @@ class Engine:
         self._check(self._L.rtg_set_tree_builder(self._h, int(builder)))
 
     @property
+    def node_width(self) -> int:
+        w = C.c_int32()
+        self._check(self._L.rtg_get_node_width(self._h, C.byref(w)))
+        return w.value
+
+    def set_node_width(self, width: int):
+        """L.RTG_NODES_AUTO (default: wide when the tree outgrows L2), L.RTG_NODES_BINARY
+        or L.RTG_NODES_WIDE (the compressed 8-wide tree); results do not depend on it."""
+        self._check(self._L.rtg_set_node_width(self._h, int(width)))
+
+    @property
     def deposit_mode(self):
         """(mode, window_factor): L.RTG_DEPOSIT_NEIGHBORS (rti's tracer) or
         L.RTG_DEPOSIT_WINDOW (rti's multi-hit window of window_factor radii)."""

@@ -58,11 +58,12 @@ def test_calibrate_global_sticking_on_hole(rtg_lib):
             r = ratio(flux(e, st, 1.0, N_RAYS, FIT_SEED))
             r.backward()  # one adjoint replay
             evals += 1
-            history.append((s, float(r), float(st.grad)))
-            if abs(float(r) - r_target) <= 1e-4 * r_target:
+            rv, dr = r.item(), st.grad.item()
+            history.append((s, rv, dr))
+            if abs(rv - r_target) <= 1e-4 * r_target:
                 break
             # Newton in log s (keeps s positive); at most a factor e^2 per step
-            s *= math.exp(max(-2.0, min(2.0, (r_target - float(r)) / (s * float(st.grad)))))
+            s *= math.exp(max(-2.0, min(2.0, (r_target - rv) / (s * dr))))
         assert evals <= 20, history
         assert abs(s - 0.01) <= 0.02 * 0.01, history
 

@@ -11,15 +11,17 @@ from rti_gb300 import scenes
 pytestmark = pytest.mark.gpu
 
 
-def _run_all(L):
+def _run_all(L, width=2):
     """Traces through the loaded library: discs with neighbours (megakernel,
-    wavefront, window deposit), triangles, an adjoint, a batch."""
+    wavefront, window deposit), triangles, an adjoint, a batch; closest hits
+    over the binary (width 2) or the compressed 8-wide tree (width 8)."""
     from rti_gb300 import Engine
     from rti_gb300.batch import Batch
     out = {}
     t = scenes.trench_discs(domain=1.2, width=0.4, depth=1.0)
     h = scenes.hole_triangles(n_theta=128, n_wall=40, n_top=8, n_bottom=6, depth=4.0)
     with Engine(0) as e:
+        e.set_node_width(width)
         e.upload_discs(t.points, t.normals, t.radii)
         e.configure(box=(t.box_lo, t.box_hi), sticking=0.1, x_bound=1, y_bound=1, reset=True)
         for name, kw in (("mk", {}), ("wf", {"scheduling": L.RTG_SCHED_WAVEFRONT}),
@@ -35,6 +37,7 @@ def _run_all(L):
         ds, dn, _ = e.adjoint(np.ones(t.n), 20000, seed=2)
         out["adjoint"] = (np.array([ds, dn]), 0)
     with Engine(0) as e:
+        e.set_node_width(width)
         e.upload_triangles(h.vertices, h.indices)
         e.configure(box=(h.box_lo, h.box_hi), sticking=0.01, reflection=2, specular_fraction=0.1, x_bound=1,
                     y_bound=1, reset=True)
@@ -48,7 +51,8 @@ def _run_all(L):
     return out
 
 
-def test_checked_build_has_no_violations_and_the_same_hits(rtg_lib):
+@pytest.mark.parametrize("width", [2, 8], ids=["binary", "wide"])
+def test_checked_build_has_no_violations_and_the_same_hits(rtg_lib, width):
     from rti_gb300 import build, _lib
     ref = _run_all(_lib)
     path = build.build(checked=True)
@@ -56,7 +60,7 @@ def test_checked_build_has_no_violations_and_the_same_hits(rtg_lib):
     _lib._lib = None
     try:
         _lib.load(path)
-        got = _run_all(_lib)
+        got = _run_all(_lib, width)
     finally:
         _lib._lib = keep
     for k, (v, err) in got.items():
