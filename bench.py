@@ -59,15 +59,18 @@ def workload():
 
 
 TREE = "karras"  # --tree
+NODE_WIDTH = 0   # --node-width: 0 automatic (binary for this L2-resident hole), 2 binary, 8 wide
 
 
-def set_tree(name):
-    global TREE
+def set_tree(name, node_width=0):
+    global TREE, NODE_WIDTH
     TREE = name
+    NODE_WIDTH = node_width
 
 
 def config_dict(h, n_rays):
     return {"workload": "hole_triangles", "radius": 0.5, "depth": 10.0, "cell": "2x2 periodic", "tree": TREE,
+            "node_width": {0: "automatic", 2: "binary", 8: "8-wide"}[NODE_WIDTH],
             "n_triangles": int(h.n), "n_rays_per_step": int(n_rays), "sticking": STICKING,
             "specular_fraction": SPECULAR, "source_exponent": 1.0, "source_plane_z": 0.1,
             "l2": "flushed between steps (256 MB write)", "parallelism": "rays sharded per rank (weak scaling)"}
@@ -319,6 +322,7 @@ def run_rough_block(args):
     rays = args.rough_rays
     with Engine(0) as e:
         e.set_tree_builder(L.RTG_TREE_PLOC)
+        e.set_node_width(NODE_WIDTH)
         t0 = time.perf_counter()
         e.upload_discs(r.points, r.normals, r.radii)
         build_s = time.perf_counter() - t0
@@ -345,12 +349,13 @@ def run_rough_block(args):
 
         fwd_ms = timed(lambda k: e.trace(rays, seed=k, stream=cs))
         t = e.tally()
+        used_width = "8-wide" if NODE_WIDTH == 8 or (NODE_WIDTH == 0 and e.uses_wide_tree) else "binary"
         adj_ms = timed(lambda k: e.adjoint_device(g.data_ptr(), 0, rays, k, fg.data_ptr(), sc.data_ptr(),
                                                   unbiased=False, stream=cs))
     return {"workload": "2048^2 discs on a Gaussian height field (rms 0.05, corr 0.2, spacing 0.01), per-disc "
                         "sticking logistic(N(-2,0.5)), cosine source, x/y periodic; L = flux onto the lowest "
                         "quarter of the discs",
-            "discs": int(r.n), "rays": rays, "tree": "PLOC", "build_s": build_s,
+            "discs": int(r.n), "rays": rays, "tree": "PLOC", "node_width": used_width, "build_s": build_s,
             "forward_ms": fwd_ms, "rays_per_s": rays / fwd_ms * 1e3, "segments": t.segments,
             "adjoint_field_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
             "grad_evals_per_s": 1e3 / (fwd_ms + adj_ms), "errors": t.errors}
@@ -375,6 +380,7 @@ def run_ours(args):
     eng = Engine(local)
     tree = L.RTG_TREE_PLOC if TREE == "ploc" else L.RTG_TREE_KARRAS
     eng.set_tree_builder(tree)
+    eng.set_node_width(NODE_WIDTH)
     eng.upload_triangles(h.vertices, h.indices)
     eng.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
                   x_bound=1, y_bound=1, source_exponent=1.0)
@@ -462,6 +468,7 @@ def run_ours(args):
         pin_s = torch.zeros(h.n, dtype=torch.float64).pin_memory().numpy()
         def e2e_step(e2, k):
             e2.set_tree_builder(tree)
+            e2.set_node_width(NODE_WIDTH)
             e2.upload_triangles(pin_v, pin_i)
             e2.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
                          x_bound=1, y_bound=1)
@@ -615,6 +622,43 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_case(args):
+    """Path-kernel time of one workload alone (the target of ncu captures):
+    hole = the bench workload, trench = the 98,301-disc trench (width 1, depth
+    5, 3 x 3 periodic cell, sticking 0.1, diffuse), rough = the 2048^2-disc
+    height field with its per-disc sticking field (PLOC tree).  Two warm-up
+    traces, then --steps traces of --rays rays; one JSON line."""
+    from rti_gb300 import Engine, scenes
+    from rti_gb300 import _lib as L
+    with Engine(0) as e:
+        e.set_node_width(args.node_width)
+        if args.case == "hole":
+            h = workload()
+            e.upload_triangles(h.vertices, h.indices)
+            e.configure(box=(h.box_lo, h.box_hi), sticking=STICKING, reflection=2, specular_fraction=SPECULAR,
+                        x_bound=1, y_bound=1, reset=True)
+        elif args.case == "trench":
+            t = scenes.trench_discs()
+            e.upload_discs(t.points, t.normals, t.radii)
+            e.configure(box=(t.box_lo, t.box_hi), sticking=0.1, x_bound=1, y_bound=1, reset=True)
+        else:
+            r = scenes.rough_discs(n=2048, spacing=0.01, rms=0.05, corr=0.2, seed=0)
+            e.set_tree_builder(L.RTG_TREE_PLOC)
+            e.upload_discs(r.points, r.normals, r.radii)
+            e.configure(box=(r.box_lo, r.box_hi), x_bound=1, y_bound=1, reset=True)
+            rng = np.random.default_rng(1)
+            e.set_sticking_field((1.0 / (1.0 + np.exp(-rng.normal(-2.0, 0.5, r.n)))).astype(np.float32))
+        rows = []
+        for k in range(2 + args.steps):
+            e.trace(args.rays, seed=k)
+            t_ = e.tally()
+            if k >= 2:
+                rows.append(t_)
+        print(json.dumps({"case": args.case, "rays": args.rays, "node_width": args.node_width,
+                          "kernel_ms": [round(t_.kernel_ms, 3) for t_ in rows], "segments": rows[-1].segments,
+                          "hitc": rows[-1].hitc, "nb_deposits": rows[-1].nb_deposits, "errors": rows[-1].errors}))
+
+
 def ray_sweep(eng, sizes):
     """Path-kernel time (best of 3) against the number of rays on the bench
     workload, and the least-squares line T = tail + slope * rays: the intercept
@@ -661,14 +705,21 @@ def main():
                                                 "(the tail analysis), printed instead of the bench line")
     ap.add_argument("--rough-rays", type=int, default=100_000_000, help="rays of the rough-surface block")
     ap.add_argument("--rough-only", action="store_true", help="run the rough-surface block alone and print it")
+    ap.add_argument("--case", default="", choices=["", "hole", "trench", "rough"],
+                    help="time the path kernel on one workload alone (--rays, --steps, --node-width)")
+    ap.add_argument("--node-width", type=int, default=0, choices=[0, 2, 8],
+                    help="tree of the closest-hit queries: 0 automatic, 2 binary, 8 compressed 8-wide")
     args = ap.parse_args()
-    set_tree(args.tree)
+    set_tree(args.tree, args.node_width)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     from __graft_entry__ import build
     if args.impl == "reference":
         from oracle import oracle
         oracle.build()
         run_reference(args)
+    elif args.case:
+        build()
+        run_case(args)
     elif args.rough_only:
         build()
         print(json.dumps(run_rough_block(args)))

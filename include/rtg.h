@@ -225,6 +225,8 @@ RTG_API int rtg_get_tree_builder(const rtg_context* ctx, int32_t* builder);
 #define RTG_NODES_WIDE 8
 RTG_API int rtg_set_node_width(rtg_context* ctx, int32_t width);
 RTG_API int rtg_get_node_width(const rtg_context* ctx, int32_t* width);
+/* The tree the closest-hit queries of the next trace use: 2 (binary) or 8. */
+RTG_API int rtg_get_traversal_width(const rtg_context* ctx, int32_t* width);
 /* What a front-face disc hit deposits.  rti has two treatments of
  * overlapping discs:
  *   RTG_DEPOSIT_NEIGHBORS (default): w*s on the hit disc and on every

@@ -46,7 +46,7 @@ EXPORTS = [
     "rtg_read_point_cloud", "rtg_read_triangles", "rtg_set_tree_builder", "rtg_get_tree_builder",
     "rtg_set_deposit_mode", "rtg_get_deposit_mode", "rtg_set_accumulation", "rtg_get_accumulation",
     "rtg_set_visit_limit", "rtg_get_visit_limit", "rtg_inject_alloc_failure", "rtg_set_node_width",
-    "rtg_get_node_width",
+    "rtg_get_node_width", "rtg_get_traversal_width",
 ]
 
 RTG_ADJ_HELD = 0
@@ -205,6 +205,7 @@ def load(path: str | None = None):
         "rtg_get_tree_builder": (C.c_int, [_ctx, _i32p]),
         "rtg_set_node_width": (C.c_int, [_ctx, C.c_int32]),
         "rtg_get_node_width": (C.c_int, [_ctx, _i32p]),
+        "rtg_get_traversal_width": (C.c_int, [_ctx, _i32p]),
         "rtg_set_deposit_mode": (C.c_int, [_ctx, C.c_int32, C.c_float]),
         "rtg_get_deposit_mode": (C.c_int, [_ctx, _i32p, _f32p]),
         "rtg_set_visit_limit": (C.c_int, [_ctx, C.c_uint64]),

@@ -781,6 +781,12 @@ int rtg_get_node_width(const rtg_context* ctx, int32_t* width) {
   return RTG_OK;
 }
 
+int rtg_get_traversal_width(const rtg_context* ctx, int32_t* width) {
+  if (!ctx || !width) return RTG_ERR_INVALID_ARGUMENT;
+  *width = use_wide(ctx) ? RTG_NODES_WIDE : RTG_NODES_BINARY;
+  return RTG_OK;
+}
+
 int rtg_set_deposit_mode(rtg_context* ctx, int32_t mode, float window_factor) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   if (mode != RTG_DEPOSIT_NEIGHBORS && mode != RTG_DEPOSIT_WINDOW)

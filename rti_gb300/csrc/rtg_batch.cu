@@ -49,6 +49,7 @@ struct rtg_batch {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int depth = 0;  // deepest LBVH among the jobs' surfaces
+  bool wide = false;  // some job's context traces over its wide tree
 };
 
 using namespace rtg;
@@ -93,7 +94,8 @@ int enqueue_batched(rtg_batch* b, cudaStream_t st, const uint64_t* prefix, uint6
   p0.tally = ctx->d_tally;
   p0.abort_flag = nullptr;
   if (total > 0)
-    RTG_TRY(launch_trace_batched(ctx, p0, b->d_jobs.p, prefix, (int)b->jobs.size(), total, st, ctx->lc, b->depth));
+    RTG_TRY(launch_trace_batched(ctx, p0, b->d_jobs.p, prefix, (int)b->jobs.size(), total, st, ctx->lc, b->depth,
+                                 b->wide));
   for (Job& j : b->jobs) RTG_TRY(compute_areas_into(j.scene, st, j.box_lo, j.box_hi, j.areas.p));
   return RTG_OK;
 }
@@ -148,7 +150,11 @@ int refresh_jobs(rtg_batch* b) {
   }
   if (changed) {
     b->depth = 0;
-    for (const Job& j : b->jobs) b->depth = std::max(b->depth, traversal_depth(j.scene));
+    b->wide = false;
+    for (const Job& j : b->jobs) {
+      b->depth = std::max(b->depth, traversal_depth(j.scene));
+      b->wide = b->wide || use_wide(j.scene);
+    }
     b->tables_ready = false;
     drop_graph(b);
   }
@@ -238,6 +244,7 @@ int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint6
   }
   b->jobs.push_back(j);
   if (traversal_depth(scene) > b->depth) b->depth = traversal_depth(scene);
+  if (use_wide(scene)) b->wide = true;
   b->tables_ready = false;
   drop_graph(b);
   if (job_out) *job_out = (int32_t)(b->jobs.size() - 1);

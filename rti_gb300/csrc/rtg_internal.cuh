@@ -271,9 +271,10 @@ int s1_to_double(rtg_context* ctx, double* s1, int64_t n, cudaStream_t st);
 bool shared_stack(rtg_context* ctx, const rtg_launch_config& lc);
 int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc);
 // trace_batched.cu: the megakernel over a job table (forward only)
+// (wide: some job's scene view carries a wide tree)
 int launch_trace_batched(rtg_context* ctx, const TraceParams& p0, const TraceParams* d_jobs, const uint64_t* d_prefix,
                          int njobs, uint64_t total_rays, cudaStream_t st, const rtg_launch_config& lc,
-                         int tree_depth);
+                         int tree_depth, bool wide);
 // wavefront.cu: the same paths scheduled as extend/shade kernel pairs over a
 // path queue (forward only; host-driven loop, not capturable)
 int launch_wavefront(rtg_context* ctx, const TraceParams& p0, const TraceParams* d_jobs, const uint64_t* d_prefix,

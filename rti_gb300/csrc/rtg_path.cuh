@@ -249,7 +249,10 @@ __device__ __forceinline__ bool closest_hit_wide(const SceneView& s, const Ray& 
 // SST = 0: the stack is a per-thread local array; SST > 0: it is a column of
 // shared memory, entry i at sstk[i * SST] (SST = the block size, so the lanes
 // of a warp always hit distinct banks).
-template <int STACK, bool POSTPONE, int SST = 0, typename Count = unsigned long long>
+// WIDE = false: the binary tree only (the wide traversal is not compiled in,
+// which keeps the binary kernels' registers); WIDE = true: the wide tree
+// whenever the scene view carries one.
+template <int STACK, bool POSTPONE, int SST = 0, bool WIDE = true, typename Count = unsigned long long>
 __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& bt, int& bid, uint32_t& bref,
                             Count& errs, uint32_t* sstk = nullptr) {
   Ray r;
@@ -260,7 +263,9 @@ __device__ bool closest_hit(const SceneView& s, f3 o, f3 d, float tnear, float& 
   bid = INT_MAX;
   bref = 0xFFFFFFFFu;
   uint32_t lstack[SST ? 1 : STACK];
-  if (!POSTPONE && s.wnodes) return closest_hit_wide<STACK, SST>(s, r, tnear, bt, bid, bref, errs, lstack, sstk);
+  if constexpr (WIDE && !POSTPONE) {
+    if (s.wnodes) return closest_hit_wide<STACK, SST>(s, r, tnear, bt, bid, bref, errs, lstack, sstk);
+  }
   auto stack = [&](int i) -> uint32_t& { return SST ? sstk[i * SST] : lstack[i]; };
   int sp = 0;
   uint32_t cur = s.root;
@@ -575,8 +580,9 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // forward traces with 128 threads target 9 blocks (56 registers, a few spilled:
 // the extra warps hide more latency than the spills cost).
 // SHSTACK = true: the traversal stacks of the block live in shared memory
-// (STACK x TPB entries, at most 16 KB).
-template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false, bool SHSTACK = false>
+// (STACK x TPB entries, at most 16 KB).  WIDE = true: closest hits over the
+// wide tree where a scene view carries one (see closest_hit).
+template <int M, bool Batched, int TPB, int STACK, bool POSTPONE = false, bool SHSTACK = false, bool WIDE = false>
 __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 : 1024) / TPB)
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
@@ -715,7 +721,7 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
     float th, tb = 0.0f;
     int hid;
     uint32_t href;
-    const bool hit = closest_hit<STACK, POSTPONE, kSst>(pp->s, o, d, pp->tnear, th, hid, href, c_err, sstk);
+    const bool hit = closest_hit<STACK, POSTPONE, kSst, WIDE>(pp->s, o, d, pp->tnear, th, hid, href, c_err, sstk);
     const int axis = boundary_exit(*pp, o, d, tb);
     if (kChecked && hit && (unsigned)hid >= (unsigned)(pp->s.nd + pp->s.nt)) {
       c_err += 1;
@@ -877,13 +883,23 @@ using PathKernel = void (*)(const TraceParams, const TraceParams*, const uint64_
 
 // The instantiation of trace_paths_kernel with its stack in shared memory
 // when `shared` asks for it and it fits 16 KB per block (8 blocks then leave
-// half of the SM's L1/shared capacity to L1), else in local memory.
-template <int M, bool Batched, int TPB, int STACK, bool POSTPONE>
-PathKernel kernel_for(bool shared) {
+// half of the SM's L1/shared capacity to L1), else in local memory; with the
+// wide traversal compiled in when `wide` (postponed leaf tests use the binary
+// tree only).
+template <int M, bool Batched, int TPB, int STACK, bool POSTPONE, bool WIDE>
+PathKernel kernel_for_width(bool shared) {
   if constexpr (STACK * TPB * 4 <= 16384) {
-    if (shared) return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, true>;
+    if (shared) return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, true, WIDE>;
   }
-  return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, false>;
+  return trace_paths_kernel<M, Batched, TPB, STACK, POSTPONE, false, WIDE>;
+}
+
+template <int M, bool Batched, int TPB, int STACK, bool POSTPONE>
+PathKernel kernel_for(bool shared, bool wide) {
+  if constexpr (!POSTPONE) {
+    if (wide) return kernel_for_width<M, Batched, TPB, STACK, false, true>(shared);
+  }
+  return kernel_for_width<M, Batched, TPB, STACK, POSTPONE, false>(shared);
 }
 
 }  // namespace

@@ -29,39 +29,44 @@ __global__ void closest_hit_kernel(const SceneView s, const float* __restrict__ 
 }
 
 template <int TPB, bool POSTPONE>
-PathKernel forward_kernel(int stack, bool shared) {
-  if (stack <= 32) return kernel_for<kModeForward, false, TPB, 32, POSTPONE>(shared);
-  if (stack <= 64) return kernel_for<kModeForward, false, TPB, 64, POSTPONE>(shared);
-  return kernel_for<kModeForward, false, TPB, 256, POSTPONE>(shared);
+PathKernel forward_kernel(int stack, bool shared, bool wide) {
+  if (stack <= 32) return kernel_for<kModeForward, false, TPB, 32, POSTPONE>(shared, wide);
+  if (stack <= 64) return kernel_for<kModeForward, false, TPB, 64, POSTPONE>(shared, wide);
+  return kernel_for<kModeForward, false, TPB, 256, POSTPONE>(shared, wide);
 }
 
 template <int TPB>
-PathKernel forward_kernel(int stack, bool postpone, bool shared) {
-  return postpone ? forward_kernel<TPB, true>(stack, shared) : forward_kernel<TPB, false>(stack, shared);
+PathKernel forward_kernel(int stack, bool postpone, bool shared, bool wide) {
+  return postpone ? forward_kernel<TPB, true>(stack, shared, wide) : forward_kernel<TPB, false>(stack, shared, wide);
 }
 
 // The adjoint replays run with 128 threads and a 64- or 256-entry stack.
-PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, bool shared, int& tpb_out) {
+PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, bool shared, bool wide, int& tpb_out) {
   if (mode == kModeAdjGlobal) {
     tpb_out = 128;
-    return stack <= 64 ? kernel_for<kModeAdjGlobal, false, 128, 64, false>(shared)
-                       : trace_paths_kernel<kModeAdjGlobal, false, 128, 256>;
+    if (stack <= 64) return kernel_for<kModeAdjGlobal, false, 128, 64, false>(shared, wide);
+    return wide ? trace_paths_kernel<kModeAdjGlobal, false, 128, 256, false, false, true>
+                : trace_paths_kernel<kModeAdjGlobal, false, 128, 256>;
   }
   if (mode == kModeAdjField) {
     tpb_out = 128;
-    return stack <= 64 ? kernel_for<kModeAdjField, false, 128, 64, false>(shared)
-                       : trace_paths_kernel<kModeAdjField, false, 128, 256>;
+    if (stack <= 64) return kernel_for<kModeAdjField, false, 128, 64, false>(shared, wide);
+    return wide ? trace_paths_kernel<kModeAdjField, false, 128, 256, false, false, true>
+                : trace_paths_kernel<kModeAdjField, false, 128, 256>;
   }
   if (mode == kModeWindow) {
     tpb_out = 128;
-    return stack <= 64 ? trace_paths_kernel<kModeWindow, false, 128, 64>
-                       : trace_paths_kernel<kModeWindow, false, 128, 256>;
+    if (stack <= 64)
+      return wide ? trace_paths_kernel<kModeWindow, false, 128, 64, false, false, true>
+                  : trace_paths_kernel<kModeWindow, false, 128, 64>;
+    return wide ? trace_paths_kernel<kModeWindow, false, 128, 256, false, false, true>
+                : trace_paths_kernel<kModeWindow, false, 128, 256>;
   }
   tpb_out = tpb;
-  if (tpb == 64) return forward_kernel<64>(stack, postpone, shared);
-  if (tpb == 256) return forward_kernel<256>(stack, postpone, shared);
+  if (tpb == 64) return forward_kernel<64>(stack, postpone, shared, wide);
+  if (tpb == 256) return forward_kernel<256>(stack, postpone, shared, wide);
   tpb_out = 128;
-  return forward_kernel<128>(stack, postpone, shared);
+  return forward_kernel<128>(stack, postpone, shared, wide);
 }
 
 }  // namespace
@@ -188,7 +193,7 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
   }
   int tpb = 128, sms = 0, per_sm = 0;
   PathKernel kern = pick_kernel(mode, lc.threads_per_block, stack, lc.leaf_tests == RTG_LEAF_POSTPONED,
-                                shared_stack(ctx, lc), tpb);
+                                shared_stack(ctx, lc), p.s.wnodes != nullptr, tpb);
   p.plain = (mode == kModeForward || mode == kModeWindow) && lc.scheduling == RTG_SCHED_PLAIN ? 1 : 0;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));

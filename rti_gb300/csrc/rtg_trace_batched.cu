@@ -7,22 +7,22 @@ namespace rtg {
 namespace {
 
 template <int TPB, bool POSTPONE>
-PathKernel batched_kernel(int stack, bool shared) {
-  if (stack <= 32) return kernel_for<kModeForward, true, TPB, 32, POSTPONE>(shared);
-  if (stack <= 64) return kernel_for<kModeForward, true, TPB, 64, POSTPONE>(shared);
-  return kernel_for<kModeForward, true, TPB, 256, POSTPONE>(shared);
+PathKernel batched_kernel(int stack, bool shared, bool wide) {
+  if (stack <= 32) return kernel_for<kModeForward, true, TPB, 32, POSTPONE>(shared, wide);
+  if (stack <= 64) return kernel_for<kModeForward, true, TPB, 64, POSTPONE>(shared, wide);
+  return kernel_for<kModeForward, true, TPB, 256, POSTPONE>(shared, wide);
 }
 
 template <int TPB>
-PathKernel batched_kernel(int stack, bool postpone, bool shared) {
-  return postpone ? batched_kernel<TPB, true>(stack, shared) : batched_kernel<TPB, false>(stack, shared);
+PathKernel batched_kernel(int stack, bool postpone, bool shared, bool wide) {
+  return postpone ? batched_kernel<TPB, true>(stack, shared, wide) : batched_kernel<TPB, false>(stack, shared, wide);
 }
 
 }  // namespace
 
 int launch_trace_batched(rtg_context* ctx, const TraceParams& p0_in, const TraceParams* d_jobs,
                          const uint64_t* d_prefix, int njobs, uint64_t total_rays, cudaStream_t st,
-                         const rtg_launch_config& lc, int tree_depth) {
+                         const rtg_launch_config& lc, int tree_depth, bool wide) {
   if (lc.scheduling == RTG_SCHED_WAVEFRONT)
     return launch_wavefront(ctx, p0_in, d_jobs, d_prefix, njobs, total_rays, st, lc, tree_depth);
   const int stack = stack_for(lc.stack_depth, tree_depth);
@@ -32,9 +32,9 @@ int launch_trace_batched(rtg_context* ctx, const TraceParams& p0_in, const Trace
   int tpb = lc.threads_per_block, sms = 0, per_sm = 0;
   const bool pp = lc.leaf_tests == RTG_LEAF_POSTPONED;
   const bool sh = lc.stack_memory == RTG_STACK_SHARED;  // AUTO: local (the jobs' trees differ in size)
-  PathKernel kern = tpb == 64    ? batched_kernel<64>(stack, pp, sh)
-                    : tpb == 256 ? batched_kernel<256>(stack, pp, sh)
-                                 : batched_kernel<128>(stack, pp, sh);
+  PathKernel kern = tpb == 64    ? batched_kernel<64>(stack, pp, sh, wide)
+                    : tpb == 256 ? batched_kernel<256>(stack, pp, sh, wide)
+                                 : batched_kernel<128>(stack, pp, sh, wide);
   if (tpb != 64 && tpb != 256) tpb = 128;
   RTG_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   RTG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, 0));

@@ -191,6 +191,13 @@ class Engine:
         self._check(self._L.rtg_get_node_width(self._h, C.byref(w)))
         return w.value
 
+    @property
+    def uses_wide_tree(self) -> bool:
+        """Whether the closest-hit queries of the next trace traverse the 8-wide tree."""
+        w = C.c_int32()
+        self._check(self._L.rtg_get_traversal_width(self._h, C.byref(w)))
+        return w.value == L.RTG_NODES_WIDE
+
     def set_node_width(self, width: int):
         """L.RTG_NODES_AUTO (default: wide when the tree outgrows L2), L.RTG_NODES_BINARY
         or L.RTG_NODES_WIDE (the compressed 8-wide tree); results do not depend on it."""

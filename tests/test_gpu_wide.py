@@ -194,6 +194,13 @@ def test_node_width_setting_and_autotune(eng):
     assert eng.node_width == L.RTG_NODES_AUTO
     with pytest.raises(RtgError, match="node width"):
         eng.set_node_width(4)
+    # automatic: a surface whose tree stays in L2 is traced over the binary tree
+    t = scenes.trench_discs(domain=1.2, width=0.4, depth=1.0)
+    eng.upload_discs(t.points, t.normals, t.radii)
+    assert not eng.uses_wide_tree
+    eng.set_node_width(L.RTG_NODES_WIDE)
+    assert eng.uses_wide_tree
+    eng.set_node_width(L.RTG_NODES_AUTO)
     h = scenes.hole_triangles(n_theta=128, n_wall=40, n_top=8, n_bottom=6, depth=4.0)
     eng.upload_triangles(h.vertices, h.indices)
     eng.configure(box=(h.box_lo, h.box_hi), sticking=0.01, x_bound=1, y_bound=1, reset=True)
