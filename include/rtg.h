@@ -340,6 +340,44 @@ RTG_API int rtg_get_tally(rtg_context* ctx, rtg_tally* out);
 /* Neighbour CSR of the discs: row_ptr (nd+1), cols (cap entries); *nnz gets the count. */
 RTG_API int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols, int64_t cap, int64_t* nnz);
 
+/* Segment log (rti's RAYLOG / RAYSRCLOG of util/ray_logger.hpp:23-71, written
+ * at trace/tracer.hpp:166,183,294-305, which record every ray segment and
+ * source point of a single-threaded run).  Here a bounded device buffer
+ * records, for the source rays [ray_begin, ray_end) of later traces, one
+ * rtg_segment per closest-hit query of their paths: the query's origin and
+ * where it ended (the hit point, the point where the path left the x/y box
+ * sideways, or where it left through the top or bottom plane; rti draws
+ * at most 10 units instead), what happened there, the primitive and the
+ * particle weight.  The source points are the origins of the segments with
+ * segment == 0.  rtg_set_segment_log(ctx, b, e, capacity) allocates room for
+ * `capacity` records (0 frees it and stops logging); every trace that does
+ * not accumulate starts the log afresh; records beyond the capacity are
+ * counted, not kept.  Logging traces run one kernel configuration of their
+ * own (results unchanged; not with RTG_DEPOSIT_WINDOW, nor in batches).
+ * rtg_get_segment_log copies up to `cap` records, sorted by (ray, segment),
+ * and reports how many were kept and how many were dropped (synchronises). */
+#define RTG_SEG_HIT 0       /* front-face primitive hit: deposit, roulette, re-emission */
+#define RTG_SEG_BACKFACE 1  /* back face: the path passes through */
+#define RTG_SEG_BOUNDARY 2  /* x/y box side: wrapped (periodic) or mirrored (reflective) */
+#define RTG_SEG_ESCAPE 3    /* left through the top or bottom plane: the path ends */
+typedef struct rtg_segment {
+  uint64_t ray;        /* source ray id */
+  uint32_t segment;    /* closest-hit query index on the path (0 = from the source plane) */
+  int32_t  kind;       /* RTG_SEG_* */
+  float    org[3];
+  float    end[3];
+  int32_t  primitive;  /* primitive id for RTG_SEG_HIT / _BACKFACE, else -1 */
+  float    weight;     /* particle weight at the segment's origin */
+} rtg_segment;
+RTG_API int rtg_set_segment_log(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t capacity);
+RTG_API int rtg_get_segment_log(rtg_context* ctx, rtg_segment* out, uint64_t cap, uint64_t* n_kept,
+                                uint64_t* n_dropped);
+/* The log as VTK XML PolyData: one line cell per segment (two points each),
+ * cell arrays ray, segment, kind, primitive, weight; the _host form writes a
+ * caller's array and needs no GPU. */
+RTG_API int rtg_write_segment_log_vtp(rtg_context* ctx, const char* path);
+RTG_API int rtg_write_vtp_segments(const char* path, const rtg_segment* seg, int64_t n);
+
 /* No counterpart in the reference.  The estimates of rtg_get_mc_estimates,
  * written to a device buffer the caller owns (d_out, one float per primitive),
  * enqueued on `stream` (NULL = the context's stream) without allocating or

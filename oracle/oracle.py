@@ -91,6 +91,8 @@ def lib():
         L.orc_adjoint.restype = C.c_int
         L.orc_adjoint.argtypes = [C.c_void_p, C.POINTER(OrcConfig), C.c_uint64, C.c_uint64, C.c_int, _f64p, C.c_int,
                                   _f64p, _f64p, _u64p]
+        L.orc_trace_log.restype = C.c_int64
+        L.orc_trace_log.argtypes = [C.c_void_p, C.POINTER(OrcConfig), C.c_uint64, C.c_void_p, C.c_int64]
         L.orc_fd_pair.restype = C.c_int
         L.orc_fd_pair.argtypes = [C.c_void_p, C.POINTER(OrcConfig), C.c_uint64, C.c_uint64, C.c_int, _f64p,
                                   C.c_float, _f64p]
@@ -263,6 +265,20 @@ def adjoint(scene: "Scene", cfg: OrcConfig, g, ray_begin: int, ray_end: int, nth
     if rc != 0:
         raise RuntimeError("orc_adjoint failed")
     return sc[0], sc[1], fg, segs.value
+
+
+SEGMENT_DTYPE = [("ray", "<u8"), ("segment", "<u4"), ("kind", "<i4"), ("org", "<f4", (3,)), ("end", "<f4", (3,)),
+                 ("primitive", "<i4"), ("weight", "<f4")]
+
+
+def trace_log(scene: "Scene", cfg: OrcConfig, ray_id: int) -> np.ndarray:
+    """Every closest-hit query of one path (orc_trace_log), in order."""
+    L = lib()
+    cfg.sticking_field = None
+    n = L.orc_trace_log(scene._h, C.byref(cfg), ray_id, None, 0)
+    out = np.zeros(n, dtype=SEGMENT_DTYPE)
+    L.orc_trace_log(scene._h, C.byref(cfg), ray_id, C.c_void_p(out.ctypes.data), n)
+    return out
 
 
 def fd_pair(scene: "Scene", cfg: OrcConfig, g, ray_begin: int, ray_end: int, h: float, nthreads: int = 0) -> dict:

@@ -625,7 +625,26 @@ typedef struct {
   uint64_t* cnt;
   orc_tally t;
   int fixed; /* s1 holds int64 multiples of 2^-32 */
+  /* segment log of one path (orc_trace_log): counted when logging, kept up to log_cap */
+  int logging;
+  orc_segment* log;
+  int64_t log_n, log_cap;
 } acc_t;
+
+static void log_seg(acc_t* a, uint64_t id, uint32_t seg, int kind, v3 o, v3 d, float t, int32_t prim, float w) {
+  if (!a->logging) return;
+  if (a->log && a->log_n < a->log_cap) {
+    orc_segment* r = &a->log[a->log_n];
+    r->ray = id;
+    r->segment = seg;
+    r->kind = kind;
+    r->org[0] = o.x; r->org[1] = o.y; r->org[2] = o.z;
+    r->end[0] = o.x + d.x * t; r->end[1] = o.y + d.y * t; r->end[2] = o.z + d.z * t;
+    r->primitive = prim;
+    r->weight = w;
+  }
+  a->log_n += 1;
+}
 
 /* hit_accumulator::use (hit_accumulator.hpp:128-138); fixed: the flux as an
  * int64 multiple of 2^-32, rounded to nearest even like the GPU */
@@ -731,9 +750,11 @@ static void trace_path(const orc_scene* s, const orc_config* cf, uint64_t id, ac
       v3 n = prim_normal(s, p);
       v3 hp = mk(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
       if (d.x * n.x + d.y * n.y + d.z * n.z > 0.0f) { /* back face: pass through */
+        log_seg(a, id, nseg - 1, 1, o, d, th, p, w);
         o = hp;
         continue;
       }
+      log_seg(a, id, nseg - 1, 0, o, d, th, p, w);
       a->t.hitc += 1;
       float st = cf->sticking_field ? cf->sticking_field[p] : cf->sticking;
       float v = w * st;
@@ -771,6 +792,7 @@ static void trace_path(const orc_scene* s, const orc_config* cf, uint64_t id, ac
       continue;
     }
     if (axis >= 0) {
+      log_seg(a, id, nseg - 1, 2, o, d, tb, -1, w);
       v3 hp = mk(o.x + d.x * tb, o.y + d.y * tb, o.z + d.z * tb);
       int periodic = axis == 0 ? cf->x_bound : cf->y_bound;
       if (periodic) {
@@ -782,6 +804,10 @@ static void trace_path(const orc_scene* s, const orc_config* cf, uint64_t id, ac
       }
       o = hp;
       continue;
+    }
+    if (a->logging) { /* out through the top or bottom plane */
+      const float tz = d.z > 0.0f ? (cf->box_hi[2] - o.z) / d.z : (d.z < 0.0f ? (cf->box_lo[2] - o.z) / d.z : 0.0f);
+      log_seg(a, id, nseg - 1, 3, o, d, tz, -1, w);
     }
     a->t.nonhitc += 1;
     break;
@@ -960,6 +986,24 @@ static void adjoint_path(const orc_scene* s, const orc_config* cf, uint64_t id, 
       return;
     }
   }
+}
+
+int64_t orc_trace_log(const orc_scene* s, const orc_config* cf, uint64_t id, orc_segment* out, int64_t cap) {
+  const int64_t np = s->np;
+  acc_t a;
+  memset(&a, 0, sizeof a);
+  a.fixed = cf->accum_fixed != 0;
+  a.s1 = (double*)calloc((size_t)np + 1, sizeof(double));
+  a.s2 = (double*)calloc((size_t)np + 1, sizeof(double));
+  a.s3 = (double*)calloc((size_t)np + 1, sizeof(double));
+  a.s4 = (double*)calloc((size_t)np + 1, sizeof(double));
+  a.cnt = (uint64_t*)calloc((size_t)np + 1, sizeof(uint64_t));
+  a.logging = 1;
+  a.log = out;
+  a.log_cap = cap;
+  trace_path(s, cf, id, &a);
+  free(a.s1); free(a.s2); free(a.s3); free(a.s4); free(a.cnt);
+  return a.log_n;
 }
 
 int orc_adjoint(const orc_scene* s, const orc_config* cf, uint64_t b, uint64_t e, int nthreads, const double* g,

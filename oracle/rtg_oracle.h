@@ -56,6 +56,20 @@ typedef struct orc_tally {
   uint64_t nb_deposits; /* neighbour deposits (tracer.hpp:371) */
 } orc_tally;
 
+/* One segment of a path (the layout of the library's segment-log record):
+ * kind 0 front-face hit, 1 back face passed, 2 x/y box side, 3 out through
+ * the top or bottom plane; end = org + t dir as the path computes its next
+ * origin. */
+typedef struct orc_segment {
+  uint64_t ray;
+  uint32_t segment;
+  int32_t kind;
+  float org[3];
+  float end[3];
+  int32_t primitive;
+  float weight;
+} orc_segment;
+
 orc_scene* orc_scene_create(const float* disc_xyzr, const float* disc_normals, int64_t n_discs,
                             const float* tri_vertices, const uint32_t* tri_indices,
                             int64_t n_vertices, int64_t n_triangles);
@@ -100,6 +114,10 @@ int orc_adjoint(const orc_scene* s, const orc_config* cf, uint64_t ray_begin, ui
  * dL/ds along the path at s.  out[8]: see rtg_oracle.c (fd_pair_path). */
 int orc_fd_pair(const orc_scene* s, const orc_config* cf, uint64_t ray_begin, uint64_t ray_end, int nthreads,
                 const double* g, float h, double* out);
+
+/* Every closest-hit query of source ray `id`'s path, in order (single
+ * thread); writes at most `cap` records, returns how many the path has. */
+int64_t orc_trace_log(const orc_scene* s, const orc_config* cf, uint64_t id, orc_segment* out, int64_t cap);
 
 /* One source ray (origin, direction) for ray id; exposes the sampler. */
 void orc_source_ray(const orc_config* cf, uint64_t id, float* org, float* dir);

@@ -46,7 +46,8 @@ EXPORTS = [
     "rtg_read_point_cloud", "rtg_read_triangles", "rtg_set_tree_builder", "rtg_get_tree_builder",
     "rtg_set_deposit_mode", "rtg_get_deposit_mode", "rtg_set_accumulation", "rtg_get_accumulation",
     "rtg_set_visit_limit", "rtg_get_visit_limit", "rtg_inject_alloc_failure", "rtg_set_node_width",
-    "rtg_get_node_width", "rtg_get_traversal_width",
+    "rtg_get_node_width", "rtg_get_traversal_width", "rtg_set_segment_log", "rtg_get_segment_log",
+    "rtg_write_segment_log_vtp", "rtg_write_vtp_segments",
 ]
 
 RTG_ADJ_HELD = 0
@@ -93,6 +94,23 @@ class RtgTally(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in
                 ("num_rays", "hitc", "nonhitc", "total", "segments", "truncated", "nb_deposits", "errors")] + [
         ("trace_ms", C.c_double), ("kernel_ms", C.c_double)]
+
+
+RTG_SEG_HIT = 0
+RTG_SEG_BACKFACE = 1
+RTG_SEG_BOUNDARY = 2
+RTG_SEG_ESCAPE = 3
+
+
+class RtgSegment(C.Structure):
+    """One record of the segment log (rtg_segment)."""
+    _fields_ = [("ray", C.c_uint64), ("segment", C.c_uint32), ("kind", C.c_int32), ("org", C.c_float * 3),
+                ("end", C.c_float * 3), ("primitive", C.c_int32), ("weight", C.c_float)]
+
+
+# numpy view of an array of RtgSegment (48 bytes each)
+SEGMENT_DTYPE = [("ray", "<u8"), ("segment", "<u4"), ("kind", "<i4"), ("org", "<f4", (3,)), ("end", "<f4", (3,)),
+                 ("primitive", "<i4"), ("weight", "<f4")]
 
 
 class RtgDeviceView(C.Structure):
@@ -206,6 +224,11 @@ def load(path: str | None = None):
         "rtg_set_node_width": (C.c_int, [_ctx, C.c_int32]),
         "rtg_get_node_width": (C.c_int, [_ctx, _i32p]),
         "rtg_get_traversal_width": (C.c_int, [_ctx, _i32p]),
+        "rtg_set_segment_log": (C.c_int, [_ctx, C.c_uint64, C.c_uint64, C.c_uint64]),
+        "rtg_get_segment_log": (C.c_int, [_ctx, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64),
+                                          C.POINTER(C.c_uint64)]),
+        "rtg_write_segment_log_vtp": (C.c_int, [_ctx, C.c_char_p]),
+        "rtg_write_vtp_segments": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int64]),
         "rtg_set_deposit_mode": (C.c_int, [_ctx, C.c_int32, C.c_float]),
         "rtg_get_deposit_mode": (C.c_int, [_ctx, _i32p, _f32p]),
         "rtg_set_visit_limit": (C.c_int, [_ctx, C.c_uint64]),

@@ -370,6 +370,7 @@ void drop_surface(rtg_context* ctx) {
   dfree(g.wnodes);
   g.n_wnodes = 0;
   g.wide_stack = 0;
+  g.wide_current = false;
   dfree(ctx->sticking_field);
   g.nd = g.nt = g.nv = 0;
   g.nb_nnz = 0;
@@ -394,6 +395,7 @@ int prepare_trace_with(rtg_context* ctx, const rtg_config& c, const float* box_l
       return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "degenerate x/y box (all discs on one line?)");
   *ctx->h_abort = 0;
   p = TraceParams{};
+  RTG_TRY(ensure_wide(ctx));
   p.s = scene_view(ctx);
   p.s1 = ctx->acc.p;
   p.s2 = ctx->acc.p + np;
@@ -526,6 +528,8 @@ int rtg_destroy(rtg_context* ctx) {
   dfree(g.refit_flags); dfree(g.nb_ptr); dfree(g.nb_idx); dfree(g.nb_slot); dfree(g.disc_slot);
   dfree(ctx->sticking_field); dfree(ctx->acc); dfree(ctx->cnt); dfree(ctx->areas); dfree(ctx->est);
   dfree(ctx->stat_tmp);
+  dfree(ctx->seglog);
+  dfree(ctx->seglog_count);
   free_wavefront(ctx->wf);
   if (ctx->d_tally) cudaFree(ctx->d_tally);
   if (ctx->d_tally_adj) cudaFree(ctx->d_tally_adj);
@@ -783,7 +787,10 @@ int rtg_get_node_width(const rtg_context* ctx, int32_t* width) {
 
 int rtg_get_traversal_width(const rtg_context* ctx, int32_t* width) {
   if (!ctx || !width) return RTG_ERR_INVALID_ARGUMENT;
-  *width = use_wide(ctx) ? RTG_NODES_WIDE : RTG_NODES_BINARY;
+  const Geometry& g = ctx->g;
+  // a wanted tree not collapsed yet is built before the next trace
+  const bool usable = !g.wide_current || (g.n_wnodes > 0 && g.wide_stack <= 256);
+  *width = wants_wide(ctx) && g.nd + g.nt > 0 && usable ? RTG_NODES_WIDE : RTG_NODES_BINARY;
   return RTG_OK;
 }
 
@@ -857,6 +864,7 @@ int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_laun
   auto run = [&](const Cand& c, float& ms) -> int {
     ctx->lc = c.lc;
     ctx->node_width = c.width;
+    RTG_TRY(ensure_wide(ctx));
     p.s = scene_view(ctx);
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->acc.p, 0, 4 * np * sizeof(double), st));
     RTG_CUDA(ctx, cudaMemsetAsync(ctx->cnt.p, 0, np * sizeof(unsigned long long), st));
@@ -968,6 +976,11 @@ int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint
   } else {
     RTG_CUDA(ctx, cudaMemsetAsync(&ctx->d_tally->next_ray, 0, sizeof(unsigned long long), st));
   }
+  if (ctx->seglog.p) {
+    if (p.window) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "the segment log records neighbour-deposit traces only");
+    p.log = SegmentLog{ctx->seglog.p, ctx->seglog.n, ctx->seglog_count.p, ctx->seglog_begin, ctx->seglog_end};
+    if (!accumulate) RTG_CUDA(ctx, cudaMemsetAsync(ctx->seglog_count.p, 0, sizeof(unsigned long long), st));
+  }
   const bool fixed = p.fixed_s1 != 0;
   if (fixed && accumulate) RTG_TRY(s1_to_fixed(ctx, ctx->acc.p, np, st));  // resume the integer sums
   RTG_CUDA(ctx, cudaEventRecord(ctx->evk0, st));
@@ -980,6 +993,65 @@ int rtg_trace_range(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint
   ctx->traced = true;
   ctx->finalized = false;
   return RTG_OK;
+}
+
+int rtg_set_segment_log(rtg_context* ctx, uint64_t ray_begin, uint64_t ray_end, uint64_t capacity) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  RTG_TRY(use_device(ctx));
+  if (capacity == 0) {
+    RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->seglog);
+    dfree(ctx->seglog_count);
+    return RTG_OK;
+  }
+  if (ray_end <= ray_begin) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "segment log: empty ray range");
+  if (capacity > (1ull << 32)) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "segment log: at most 2^32 records");
+  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  RTG_TRY(dalloc(ctx, ctx->seglog, (size_t)capacity, "segment log"));
+  RTG_TRY(dalloc(ctx, ctx->seglog_count, 1, "segment log counter"));
+  RTG_CUDA(ctx, cudaMemsetAsync(ctx->seglog_count.p, 0, sizeof(unsigned long long), ctx->stream));
+  ctx->seglog_begin = ray_begin;
+  ctx->seglog_end = ray_end;
+  return RTG_OK;
+}
+
+// The kept records, sorted by (ray, segment); *dropped = records that did not fit.
+static int read_segment_log(rtg_context* ctx, std::vector<rtg_segment>& out, uint64_t* dropped) {
+  out.clear();
+  if (dropped) *dropped = 0;
+  if (!ctx->seglog.p) return RTG_OK;
+  RTG_TRY(use_device(ctx));
+  RTG_CUDA(ctx, cudaDeviceSynchronize());
+  unsigned long long count = 0;
+  RTG_CUDA(ctx, cudaMemcpy(&count, ctx->seglog_count.p, sizeof count, cudaMemcpyDeviceToHost));
+  const uint64_t kept = std::min<uint64_t>(count, ctx->seglog.n);
+  out.resize(kept);
+  if (kept) RTG_CUDA(ctx, cudaMemcpy(out.data(), ctx->seglog.p, kept * sizeof(rtg_segment), cudaMemcpyDeviceToHost));
+  std::sort(out.begin(), out.end(), [](const rtg_segment& a, const rtg_segment& b) {
+    return a.ray != b.ray ? a.ray < b.ray : a.segment < b.segment;
+  });
+  if (dropped) *dropped = count - kept;
+  return RTG_OK;
+}
+
+int rtg_get_segment_log(rtg_context* ctx, rtg_segment* out, uint64_t cap, uint64_t* n_kept, uint64_t* n_dropped) {
+  if (!ctx || (cap > 0 && !out)) return RTG_ERR_INVALID_ARGUMENT;
+  std::vector<rtg_segment> v;
+  uint64_t dropped = 0;
+  RTG_TRY(read_segment_log(ctx, v, &dropped));
+  if (!v.empty() && cap > 0) std::memcpy(out, v.data(), std::min<uint64_t>(cap, v.size()) * sizeof(rtg_segment));
+  if (n_kept) *n_kept = v.size();
+  if (n_dropped) *n_dropped = dropped;
+  return RTG_OK;
+}
+
+int rtg_write_segment_log_vtp(rtg_context* ctx, const char* path) {
+  if (!ctx || !path) return RTG_ERR_INVALID_ARGUMENT;
+  if (!ctx->seglog.p) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "no segment log (rtg_set_segment_log)");
+  std::vector<rtg_segment> v;
+  RTG_TRY(read_segment_log(ctx, v, nullptr));
+  const int rc = rtg_write_vtp_segments(path, v.data(), (int64_t)v.size());
+  return rc == RTG_OK ? rc : set_error(ctx, rc, std::string("cannot write ") + path);
 }
 
 int rtg_set_sticking_field_device(rtg_context* ctx, const float* d_field, int64_t n, void* stream) {

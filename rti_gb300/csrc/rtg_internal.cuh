@@ -84,6 +84,15 @@ struct SceneView {
   uint32_t max_visits;
 };
 
+// The segment log of a trace (rtg_set_segment_log): records of the source
+// rays [ray_begin, ray_end), rec == nullptr when off.
+struct SegmentLog {
+  rtg_segment* rec;
+  unsigned long long cap;
+  unsigned long long* count;  // records asked for (kept: min(count, cap))
+  uint64_t ray_begin, ray_end;
+};
+
 struct TraceParams {
   SceneView s;
   // accumulators by original primitive id
@@ -118,6 +127,7 @@ struct TraceParams {
   double* adj_scalars;     // [0] dL/ds (global sticking), [1] dL/dn (source exponent)
   double adj_inv_n1;       // 1 / (n + 1)
   int32_t adj_unbiased;    // 0: roulette decisions held as drawn; 1: with their likelihood ratio
+  SegmentLog log;          // forward traces (kModeLogged)
 };
 
 // Path-kernel modes: the forward trace, and two adjoint replays of the same
@@ -126,6 +136,7 @@ constexpr int kModeForward = 0;
 constexpr int kModeAdjGlobal = 1;  // dL/ds (one global sticking) and dL/dn
 constexpr int kModeAdjField = 2;   // dL/ds_j (sticking field) and dL/dn
 constexpr int kModeWindow = 3;     // forward trace with the multi-hit window deposit
+constexpr int kModeLogged = 4;     // forward trace that also fills the segment log
 
 // ---- device buffers owned by a context ----
 template <typename T>
@@ -166,6 +177,7 @@ struct Geometry {
   DBuf<WideNode> wnodes;
   uint32_t n_wnodes = 0;
   int32_t wide_stack = 0;  // traversal stack entries the wide tree can need
+  bool wide_current = false;  // wnodes were collapsed from the current binary tree (n_wnodes 0: unusable)
 };
 
 // Wavefront scheduling state (device buffers, lazily allocated).
@@ -197,6 +209,10 @@ struct rtg_context {
   rtg::DBuf<float> areas;
   rtg::DBuf<float> est;
   rtg::DBuf<double> stat_tmp;
+  // segment log (rtg_set_segment_log)
+  rtg::DBuf<rtg_segment> seglog;
+  rtg::DBuf<unsigned long long> seglog_count;
+  uint64_t seglog_begin = 0, seglog_end = 0;
   rtg::DevTally* d_tally = nullptr;
   rtg::DevTally* d_tally_adj = nullptr;  // counters of adjoint replays
   uint32_t* h_abort = nullptr;  // host-mapped flag
@@ -240,8 +256,13 @@ int radix_sort_pairs(rtg_context* ctx, uint32_t* d_keys, uint32_t* d_vals, uint3
 // lbvh.cu
 int build_lbvh(rtg_context* ctx);      // full build from the by-id primitive data
 int refit_lbvh(rtg_context* ctx);      // recompute boxes, keep topology
-// wide.cu: the 8-wide compressed tree from the binary one (after a build or refit)
+// wide.cu: the 8-wide compressed tree from the binary one (after a build or
+// refit when the context wants it, else before the first trace that does)
 int build_wide(rtg_context* ctx, cudaStream_t st);
+// whether the node width setting asks for the wide tree on this surface
+bool wants_wide(const rtg_context* ctx);
+// collapses the wide tree if it is wanted and not current (synchronises)
+int ensure_wide(rtg_context* ctx);
 // surface.cu
 int build_neighbors(rtg_context* ctx);
 int compute_areas(rtg_context* ctx, cudaStream_t st, const float* box_lo, const float* box_hi);

@@ -623,7 +623,8 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
   if (np == 1) {
     single_leaf_kernel<<<1, 1, 0, st>>>(g.leaf_ref.p, g.disc.p, g.tri.p, g.prim_lo.p, g.prim_hi.p, g.nodes.p);
     RTG_CUDA(ctx, cudaGetLastError());
-    return build_wide(ctx, st);
+    g.wide_current = false;
+    return wants_wide(ctx) ? build_wide(ctx, st) : RTG_OK;
   }
   DBuf<float> node_box;
   DBuf<unsigned long long> err;
@@ -648,7 +649,8 @@ int run_slots_and_refit(rtg_context* ctx, const uint32_t* d_sorted_prim, const u
   tfree(err, st);
   if (e != cudaSuccess) return check_cuda(ctx, e, "LBVH refit");
   if (herr) return set_error(ctx, RTG_ERR_INTERNAL, "LBVH refit exceeded its depth limit");
-  return build_wide(ctx, st);  // the wide tree's boxes follow the binary ones
+  g.wide_current = false;  // the wide tree's boxes follow the binary ones: now, or before a trace that wants it
+  return wants_wide(ctx) ? build_wide(ctx, st) : RTG_OK;
 }
 
 }  // namespace

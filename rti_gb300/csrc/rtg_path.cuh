@@ -538,6 +538,29 @@ __device__ __forceinline__ int boundary_exit(const TraceParams& p, f3 o, f3 d, f
   return axis;
 }
 
+// One record of the segment log (rtg_set_segment_log) for a logged ray: the
+// query from o along d that ended at distance t.  A full log counts the
+// record without keeping it.
+__device__ __noinline__ void log_segment(const SegmentLog& lg, uint64_t id, uint32_t seg, int kind, f3 o, f3 d,
+                                         float t, int prim, float w) {
+  if (id < lg.ray_begin || id >= lg.ray_end) return;
+  const unsigned long long i = atomicAdd(lg.count, 1ull);
+  if (i >= lg.cap) return;
+  rtg_segment r;
+  r.ray = id;
+  r.segment = seg;
+  r.kind = kind;
+  r.org[0] = o.x;
+  r.org[1] = o.y;
+  r.org[2] = o.z;
+  r.end[0] = o.x + d.x * t;  // as the path computes its next origin
+  r.end[1] = o.y + d.y * t;
+  r.end[2] = o.z + d.z * t;
+  r.primitive = prim;
+  r.weight = w;
+  lg.rec[i] = r;
+}
+
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
@@ -587,6 +610,7 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
     trace_paths_kernel(const __grid_constant__ TraceParams p0, const TraceParams* __restrict__ jobs,
                        const uint64_t* __restrict__ prefix, int njobs) {
   constexpr bool kAdj = M == kModeAdjGlobal || M == kModeAdjField;
+  constexpr bool kLog = M == kModeLogged;  // a forward trace that also fills p0.log
   static_assert(!SHSTACK || STACK * TPB * 4 <= 16384, "a shared stack of at most 16 KB per block");
   constexpr int kSst = SHSTACK ? TPB : 0;
   uint32_t* sstk = nullptr;
@@ -735,9 +759,11 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
       const f3 n = mk3(nn.x, nn.y, nn.z);
       const f3 hp = mk3(o.x + d.x * th, o.y + d.y * th, o.z + d.z * th);
       if (d.x * n.x + d.y * n.y + d.z * n.z > 0.0f) {  // back face: pass through (tracer.hpp:216-227)
+        if (kLog) log_segment(p0.log, id, nseg - 1, RTG_SEG_BACKFACE, o, d, th, hid, w);
         o = hp;
         continue;
       }
+      if (kLog) log_segment(p0.log, id, nseg - 1, RTG_SEG_HIT, o, d, th, hid, w);
       c_hit += 1;
       const float st = pp->s.sticking_field ? __ldg(&pp->s.sticking_field[hid]) : pp->sticking;
       const float v = w * st;
@@ -842,6 +868,7 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
       continue;
     }
     if (axis >= 0) {  // boundary_x_y::process_hit (boundary_x_y.hpp:92-143)
+      if (kLog) log_segment(p0.log, id, nseg - 1, RTG_SEG_BOUNDARY, o, d, tb, -1, w);
       f3 hp = mk3(o.x + d.x * tb, o.y + d.y * tb, o.z + d.z * tb);
       const int periodic = axis == 0 ? pp->x_periodic : pp->y_periodic;
       if (periodic) {
@@ -853,6 +880,10 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
       }
       o = hp;
       continue;
+    }
+    if (kLog) {  // out through the top or bottom plane
+      const float tz = d.z > 0.0f ? (pp->box_hi[2] - o.z) / d.z : (d.z < 0.0f ? (pp->box_lo[2] - o.z) / d.z : 0.0f);
+      log_segment(p0.log, id, nseg - 1, RTG_SEG_ESCAPE, o, d, tz, -1, w);
     }
     c_non += 1;
     active = path_end();

@@ -54,6 +54,10 @@ PathKernel pick_kernel(int mode, int tpb, int stack, bool postpone, bool shared,
     return wide ? trace_paths_kernel<kModeAdjField, false, 128, 256, false, false, true>
                 : trace_paths_kernel<kModeAdjField, false, 128, 256>;
   }
+  if (mode == kModeLogged) {  // a debugging trace: one configuration, both trees
+    tpb_out = 128;
+    return trace_paths_kernel<kModeLogged, false, 128, 256, false, false, true>;
+  }
   if (mode == kModeWindow) {
     tpb_out = 128;
     if (stack <= 64)
@@ -142,9 +146,8 @@ int check_launch_config(rtg_context* ctx, const rtg_launch_config& lc) {
 }
 
 bool use_wide(const rtg_context* ctx) {
-  if (ctx->g.n_wnodes == 0 || ctx->g.wide_stack > 256) return false;
-  if (ctx->node_width == RTG_NODES_AUTO) return outgrows_l2(ctx);
-  return ctx->node_width == RTG_NODES_WIDE;
+  const Geometry& g = ctx->g;
+  return g.wide_current && g.n_wnodes > 0 && g.wide_stack <= 256 && wants_wide(ctx);
 }
 
 int traversal_depth(const rtg_context* ctx) {
@@ -178,8 +181,10 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
   TraceParams p = p_in;
   p.packet = lc.packet;
   const uint64_t nrays = p.ray_end - p.ray_begin;
-  // the window deposit has a kernel of its own (megakernel or plain schedule)
+  // the window deposit has a kernel of its own (megakernel or plain schedule),
+  // so has a trace that fills the segment log
   if (mode == kModeForward && p.window) mode = kModeWindow;
+  if (mode == kModeForward && p.log.rec) mode = kModeLogged;
   if (mode == kModeForward && lc.scheduling == RTG_SCHED_WAVEFRONT) {
     // a job table of one entry
     Wavefront& wf = ctx->wf;
@@ -210,6 +215,7 @@ int launch_trace(rtg_context* ctx, const TraceParams& p_in, cudaStream_t st, int
 int launch_closest_hit(rtg_context* ctx, const float* d_rays, int64_t n, float tnear, int32_t* d_prim, float* d_t,
                        unsigned long long* d_errors, cudaStream_t st) {
   if (n <= 0) return RTG_OK;
+  RTG_TRY(ensure_wide(ctx));
   SceneView s = scene_view(ctx);
   closest_hit_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, d_rays, n, tnear, d_prim, d_t, d_errors);
   RTG_CUDA(ctx, cudaGetLastError());

@@ -531,6 +531,45 @@ void set_err(char* buf, int32_t len, const std::string& m) {
 
 extern "C" {
 
+int rtg_write_vtp_segments(const char* path, const rtg_segment* seg, int64_t n) {
+  if (!path || n < 0 || (n > 0 && !seg)) return RTG_ERR_INVALID_ARGUMENT;
+  Out o;
+  o.f = std::fopen(path, "w");
+  if (!o.f) return RTG_ERR_INVALID_ARGUMENT;
+  o.put("<?xml version=\"1.0\"?>\n");
+  o.put("<VTKFile type=\"PolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n");
+  o.put("  <PolyData>\n");
+  o.fmt("    <Piece NumberOfPoints=\"%lld\" NumberOfVerts=\"0\" NumberOfLines=\"%lld\" NumberOfStrips=\"0\" "
+        "NumberOfPolys=\"0\">\n",
+        (long long)(2 * n), (long long)n);
+  o.put("      <PointData>\n      </PointData>\n");
+  o.put("      <CellData>\n");
+  data_array(o, "UInt64", "ray", 1, n, "%llu", [&](int64_t i) { return (unsigned long long)seg[i].ray; });
+  data_array(o, "UInt32", "segment", 1, n, "%u", [&](int64_t i) { return (unsigned)seg[i].segment; });
+  data_array(o, "Int32", "kind", 1, n, "%d", [&](int64_t i) { return (int)seg[i].kind; });
+  data_array(o, "Int32", "primitive", 1, n, "%d", [&](int64_t i) { return (int)seg[i].primitive; });
+  data_array(o, "Float32", "weight", 1, n, "%.9g", [&](int64_t i) { return (double)seg[i].weight; });
+  o.put("      </CellData>\n");
+  o.put("      <Points>\n");
+  data_array(o, "Float32", "Points", 3, 2 * n, "%.9g", [&](int64_t i) -> double {
+    const int64_t pt = i / 3, a = i % 3;
+    const rtg_segment& s = seg[pt / 2];
+    return (double)((pt & 1) ? s.end[a] : s.org[a]);
+  });
+  o.put("      </Points>\n");
+  for (const char* sec : {"Verts", "Lines", "Strips", "Polys"}) {
+    const bool lines = sec[0] == 'L';
+    o.fmt("      <%s>\n", sec);
+    data_array(o, "Int64", "connectivity", 1, lines ? 2 * n : 0, "%lld", [&](int64_t i) { return (long long)i; });
+    data_array(o, "Int64", "offsets", 1, lines ? n : 0, "%lld", [&](int64_t i) { return (long long)(2 * (i + 1)); });
+    o.fmt("      </%s>\n", sec);
+  }
+  o.put("    </Piece>\n  </PolyData>\n</VTKFile>\n");
+  const bool ok = o.ok;
+  if (std::fclose(o.f) != 0 || !ok) return RTG_ERR_INTERNAL;
+  return RTG_OK;
+}
+
 int rtg_write_vtp_discs(const char* path, int64_t n, const float* points, const float* normals, const float* radii,
                         const double* value, const uint64_t* hitcnt, const float* exposed_area,
                         const double* relative_error, const double* vov, const char* const* meta_keys,

@@ -226,11 +226,22 @@ __global__ void wide_init_kernel(uint32_t* w2b, uint32_t* need, unsigned int* ct
 
 }  // namespace
 
+bool wants_wide(const rtg_context* ctx) {
+  return ctx->node_width == RTG_NODES_WIDE || (ctx->node_width == RTG_NODES_AUTO && outgrows_l2(ctx));
+}
+
+int ensure_wide(rtg_context* ctx) {
+  const Geometry& g = ctx->g;
+  if (g.wide_current || g.nd + g.nt == 0 || !g.nodes.p || !wants_wide(ctx)) return RTG_OK;
+  return build_wide(ctx, ctx->stream);
+}
+
 int build_wide(rtg_context* ctx, cudaStream_t st) {
   Geometry& g = ctx->g;
   const int64_t np = g.nd + g.nt;
   g.n_wnodes = 0;
   g.wide_stack = 0;
+  g.wide_current = false;
   if (np <= 0) return RTG_OK;
   const uint32_t n_bin = (uint32_t)(np > 1 ? np - 1 : 1);  // binary internal nodes (one for a single primitive)
   RTG_TRY(dalloc(ctx, g.wnodes, (size_t)n_bin, "wide tree"));
@@ -259,6 +270,7 @@ int build_wide(rtg_context* ctx, cudaStream_t st) {
   cleanup();
   if (e != cudaSuccess) return check_cuda(ctx, e, "wide tree");
   if (h[0] != h[2]) return set_error(ctx, RTG_ERR_INTERNAL, "wide tree deeper than the binary tree");
+  g.wide_current = true;
   if (h[4] != 0) return RTG_OK;  // a node too wide for the byte grid: closest hits use the binary tree
   g.n_wnodes = h[2];
   g.wide_stack = (int32_t)h[3];

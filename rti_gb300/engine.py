@@ -191,6 +191,27 @@ class Engine:
         self._check(self._L.rtg_get_node_width(self._h, C.byref(w)))
         return w.value
 
+    # -- segment log (rti's RAYLOG / RAYSRCLOG) -------------------------------
+    def set_segment_log(self, ray_begin: int, ray_end: int, capacity: int):
+        """Record every closest-hit query of the source rays [ray_begin, ray_end)
+        of later traces, up to `capacity` records; capacity 0 stops logging."""
+        self._check(self._L.rtg_set_segment_log(self._h, int(ray_begin), int(ray_end), int(capacity)))
+
+    def segment_log(self):
+        """(records, dropped): a numpy structured array (L.SEGMENT_DTYPE) sorted by
+        (ray, segment), and the number of records that did not fit."""
+        kept, dropped = C.c_uint64(), C.c_uint64()
+        self._check(self._L.rtg_get_segment_log(self._h, None, 0, C.byref(kept), C.byref(dropped)))
+        out = np.zeros(kept.value, dtype=L.SEGMENT_DTYPE)
+        assert out.dtype.itemsize == C.sizeof(L.RtgSegment)
+        self._check(self._L.rtg_get_segment_log(self._h, C.c_void_p(out.ctypes.data), kept.value, C.byref(kept),
+                                                C.byref(dropped)))
+        return out[:kept.value], dropped.value
+
+    def write_segment_log(self, path: str):
+        """The segment log as VTK XML PolyData (one line cell per segment)."""
+        self._check(self._L.rtg_write_segment_log_vtp(self._h, str(path).encode()))
+
     @property
     def uses_wide_tree(self) -> bool:
         """Whether the closest-hit queries of the next trace traverse the 8-wide tree."""

@@ -75,6 +75,9 @@ int main(void) {
   printf("rtg_launch_config %zu\n", sizeof(rtg_launch_config));
   F(rtg_launch_config, packet); F(rtg_launch_config, stack_depth); F(rtg_launch_config, scheduling);
   F(rtg_launch_config, leaf_tests); F(rtg_launch_config, stack_memory);
+  printf("rtg_segment %zu\n", sizeof(rtg_segment));
+  F(rtg_segment, segment); F(rtg_segment, kind); F(rtg_segment, org); F(rtg_segment, end);
+  F(rtg_segment, primitive); F(rtg_segment, weight);
   return 0;
 }
 """
@@ -89,13 +92,15 @@ def test_struct_layout_matches_ctypes(tmp_path):
     out = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                               check=True).stdout.split("\n") if line)
     structs = {"rtg_config": _lib.RtgConfig, "rtg_tally": _lib.RtgTally, "rtg_device_view": _lib.RtgDeviceView,
-               "rtg_launch_config": _lib.RtgLaunchConfig}
+               "rtg_launch_config": _lib.RtgLaunchConfig, "rtg_segment": _lib.RtgSegment}
     for key, val in out.items():
         if "." in key:
             s, m = key.split(".")
             assert getattr(structs[s], m).offset == int(val), key
         else:
             assert C.sizeof(structs[key]) == int(val), key
+    import numpy as np
+    assert np.dtype(_lib.SEGMENT_DTYPE).itemsize == C.sizeof(_lib.RtgSegment) == 48
 
 
 def test_cpp_dropin_header_compiles(tmp_path):

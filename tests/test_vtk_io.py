@@ -218,3 +218,36 @@ def test_reader_errors(tmp_path):
                        ("Points", "Points", p.astype(np.float64).ravel(), 3)], "binary")
     with pytest.raises(RtgError, match="radius"):
         vtk.read_point_cloud(str(f))
+
+
+def test_segment_log_vtp_writer(rtg_lib, tmp_path):
+    """rtg_write_vtp_segments (no GPU): one line cell per segment, two points
+    each (origin, end), the cell arrays in record order."""
+    import ctypes as C
+
+    from rti_gb300 import _lib as L
+    seg = np.zeros(3, dtype=L.SEGMENT_DTYPE)
+    seg["ray"] = [7, 7, 9]
+    seg["segment"] = [0, 1, 0]
+    seg["kind"] = [L.RTG_SEG_HIT, L.RTG_SEG_ESCAPE, L.RTG_SEG_BOUNDARY]
+    seg["org"] = [[0, 0, 1], [0.5, 0.5, 0], [1, 1, 1]]
+    seg["end"] = [[0.5, 0.5, 0], [0.25, 0.75, 1], [2, 1, 1]]
+    seg["primitive"] = [4, -1, -1]
+    seg["weight"] = [1.0, 0.99, 1.0]
+    f = tmp_path / "log.vtp"
+    assert rtg_lib.rtg_write_vtp_segments(str(f).encode(), C.c_void_p(seg.ctypes.data), 3) == 0
+    piece = ET.parse(f).getroot().find("PolyData/Piece")
+    assert piece.get("NumberOfLines") == "3" and piece.get("NumberOfPoints") == "6"
+    _, _, cells = _cell_arrays(f)
+    assert cells["ray"][0] == "UInt64" and cells["kind"][0] == "Int32"
+    np.testing.assert_array_equal(cells["ray"][2], [7, 7, 9])
+    np.testing.assert_array_equal(cells["kind"][2], seg["kind"])
+    np.testing.assert_array_equal(cells["primitive"][2], [4, -1, -1])
+    np.testing.assert_allclose(cells["weight"][2], seg["weight"])
+    pts = np.array(piece.find("Points/DataArray").text.split(), dtype=np.float64).reshape(-1, 3)
+    np.testing.assert_allclose(pts[0::2], seg["org"])
+    np.testing.assert_allclose(pts[1::2], seg["end"])
+    lines = piece.find("Lines")
+    conn = np.array(lines.findall("DataArray")[0].text.split(), dtype=np.int64)
+    np.testing.assert_array_equal(conn, np.arange(6))
+    assert rtg_lib.rtg_write_vtp_segments(None, None, 0) == L.RTG_ERR_INVALID_ARGUMENT
