@@ -3,6 +3,7 @@
 //
 //   rtg --infile surface.vtp [--outfile out.vtp] [--number-of-rays N]
 //       [--sticking S] [--triangles | --discs] [--seed K] [--device D]
+//       [--ray-log N]
 //
 // As dev.cpp: the surface is read from a VTK XML file, the x/y box spans the
 // disc centres and is periodic on both axes, the source plane lies at the
@@ -14,7 +15,10 @@
 // side walls of the box as triangles.  Differences: --triangles traces a
 // triangle mesh (dev.cpp rejects it); --max-threads and --single-hit are
 // accepted and ignored (the GPU sets its own parallelism; dev.cpp parses
-// --single-hit without using it).
+// --single-hit without using it).  --ray-log N writes raylog.vtp with every
+// segment of the paths of the first N source rays (what dev.cpp writes when
+// rti is compiled with RAYLOG_ON, ray_logger.hpp:23-71; their segment-0
+// origins are RAYSRCLOG's source points).
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -34,13 +38,14 @@ struct Options {
   bool triangles = false;
   unsigned long long seed = 0;
   int device = 0;
+  unsigned long long ray_log = 0;  // source rays whose segments go to raylog.vtp
 };
 
 void usage(const char* argv0) {
   std::printf(
       "usage: %s --infile|-i FILE.vtp [--outfile|-o FILE.vtp] [--number-of-rays|--n-rays|-r N]\n"
       "          [--sticking-coefficient|--sticking-c|--sticking|-s S] [--triangles|--discs]\n"
-      "          [--seed K] [--device D] [--max-threads|-m N] [--single-hit|--single]\n",
+      "          [--seed K] [--device D] [--max-threads|-m N] [--single-hit|--single] [--ray-log N]\n",
       argv0);
 }
 
@@ -81,6 +86,9 @@ bool parse(int argc, char** argv, Options& o) {
     } else if (is(a, {"--seed"})) {
       if (!value(v)) return false;
       o.seed = std::strtoull(v.c_str(), nullptr, 10);
+    } else if (is(a, {"--ray-log"})) {
+      if (!value(v)) return false;
+      o.ray_log = std::strtoull(v.c_str(), nullptr, 10);
     } else if (is(a, {"--device"})) {
       if (!value(v)) return false;
       o.device = std::atoi(v.c_str());
@@ -199,6 +207,10 @@ int main(int argc, char** argv) {
     cfg.box_hi[a] = hi[a];
   }
   if (rtg_set_config(ctx, &cfg) != RTG_OK) return fail(ctx, "configuration");
+  // room for long paths: 2^16 segments per logged ray, at most 2^26 records
+  if (o.ray_log > 0 &&
+      rtg_set_segment_log(ctx, 0, o.ray_log, std::min<unsigned long long>(o.ray_log << 16, 1ull << 26)) != RTG_OK)
+    return fail(ctx, "ray log");
   if (rtg_trace(ctx, o.rays, o.seed, nullptr) != RTG_OK) return fail(ctx, "trace");
   rtg_tally t;
   if (rtg_get_tally(ctx, &t) != RTG_OK) return fail(ctx, "trace");
@@ -207,6 +219,10 @@ int main(int argc, char** argv) {
               o.infile.c_str(), (unsigned long long)t.num_rays, t.trace_ms * 1e-3, (unsigned long long)t.hitc,
               (unsigned long long)t.nonhitc, (unsigned long long)t.segments);
 
+  if (o.ray_log > 0) {
+    std::printf("Writing ray log to raylog.vtp\n");
+    if (rtg_write_segment_log_vtp(ctx, "raylog.vtp") != RTG_OK) return fail(ctx, "ray log");
+  }
   if (!o.outfile.empty()) {
     if (extension(o.outfile) != ".vtp") {
       std::printf("Appending .vtp to the given file name\n");

@@ -47,8 +47,8 @@ def test_cli_trace_matches_binding(cli, tmp_path):
     inp = tmp_path / "trench.vtp"
     vtk.write_vtp_discs(str(inp), t.points, t.normals, t.radii)
     out = tmp_path / "res"
-    r = subprocess.run([cli, "-i", str(inp), "-o", str(out), "-r", "200000", "-s", "0.1", "--seed", "3"],
-                       capture_output=True, text=True)
+    r = subprocess.run([cli, "-i", str(inp), "-o", str(out), "-r", "200000", "-s", "0.1", "--seed", "3",
+                        "--ray-log", "20"], capture_output=True, text=True, cwd=str(tmp_path))
     assert r.returncode == 0, r.stderr
     assert os.path.exists(str(out) + ".vtp") and os.path.exists(str(out) + ".bounding-box.vtp")
     cells = _cells(str(out) + ".vtp")
@@ -64,7 +64,15 @@ def test_cli_trace_matches_binding(cli, tmp_path):
         np.testing.assert_allclose(cells["value"], e.values(), rtol=1e-15)
         np.testing.assert_allclose(cells["exposed-area"], e.exposed_areas(), rtol=1e-7)
         np.testing.assert_allclose(cells["relative-error"], e.relative_error(), rtol=1e-12, atol=1e-300)
+        # the ray log of the first 20 rays (rti's raylog.vtp) equals the binding's segment log
+        e.set_segment_log(0, 20, 1 << 20)
+        e.trace(200000, seed=3)
+        log, _ = e.segment_log()
     assert cells["hitcnt"].sum() > 0
+    piece = ET.parse(tmp_path / "raylog.vtp").getroot().find("PolyData/Piece")
+    assert int(piece.get("NumberOfLines")) == len(log) > 20
+    pts = np.array(piece.find("Points/DataArray").text.split(), dtype=np.float32).reshape(-1, 3)
+    np.testing.assert_array_equal(pts[0::2], log["org"])
     v, tri = vtk.read_triangles(str(out) + ".bounding-box.vtp")
     assert v.shape == (8, 3) and tri.shape == (8, 3)
 
