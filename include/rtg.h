@@ -340,6 +340,30 @@ RTG_API int rtg_get_tally(rtg_context* ctx, rtg_tally* out);
 /* Neighbour CSR of the discs: row_ptr (nd+1), cols (cap entries); *nnz gets the count. */
 RTG_API int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols, int64_t cap, int64_t* nnz);
 
+/* The special-purpose VTU readers of rti (UnstructuredGrid point clouds and
+ * meshes written by other simulators):
+ *   RTG_VTU_AREA (io/christoph/vtu_point_cloud_reader.hpp:31-120): radius =
+ *     sqrt(point data "area_around_vertex", else cell data "gridSpacing")
+ *     x sqrt(3)/2 x 1.25; normals from cell data "Normals", else point data
+ *     "normal_vector"; the z coordinates of points and normals inverted;
+ *   RTG_VTU_SPACING (io/xaver/vtu_point_cloud_reader.hpp:30-110): radius =
+ *     cell data "gridSpacing" x sqrt(3)/2 x 1.25, z kept.
+ * Both leave out points of zero area (radius) or with the zero vector as
+ * normal and normalise the others' normals (utils.hpp:77-93); *n gets the
+ * number kept (all outputs NULL: count only).  rtg_read_triangles_vtu is
+ * io/christoph/vtu_triangle_reader.hpp:29-105: every three-point cell with its
+ * second and third vertex swapped and, in `normals` (may be NULL), the mean
+ * of its vertices' "normal_vector" values, normalised -- (0, 0, 1) where
+ * all three components are below 1e-5, as the reference tests them (signed).
+ * Where the reference would dereference a missing array, these return
+ * RTG_ERR_INVALID_ARGUMENT with a message in err. */
+#define RTG_VTU_AREA 1
+#define RTG_VTU_SPACING 2
+RTG_API int rtg_read_point_cloud_vtu(const char* path, int32_t flavor, int64_t* n, float* points, float* normals,
+                                     float* radii, char* err, int32_t err_len);
+RTG_API int rtg_read_triangles_vtu(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices,
+                                   float* normals, char* err, int32_t err_len);
+
 /* Segment log (rti's RAYLOG / RAYSRCLOG of util/ray_logger.hpp:23-71, written
  * at trace/tracer.hpp:166,183,294-305, which record every ray segment and
  * source point of a single-threaded run).  Here a bounded device buffer

@@ -47,7 +47,7 @@ EXPORTS = [
     "rtg_set_deposit_mode", "rtg_get_deposit_mode", "rtg_set_accumulation", "rtg_get_accumulation",
     "rtg_set_visit_limit", "rtg_get_visit_limit", "rtg_inject_alloc_failure", "rtg_set_node_width",
     "rtg_get_node_width", "rtg_get_traversal_width", "rtg_set_segment_log", "rtg_get_segment_log",
-    "rtg_write_segment_log_vtp", "rtg_write_vtp_segments",
+    "rtg_write_segment_log_vtp", "rtg_write_vtp_segments", "rtg_read_point_cloud_vtu", "rtg_read_triangles_vtu",
 ]
 
 RTG_ADJ_HELD = 0
@@ -66,6 +66,8 @@ RTG_ACCUM_FP64 = 0
 RTG_ACCUM_FIXED = 1
 RTG_DEPOSIT_NEIGHBORS = 0
 RTG_DEPOSIT_WINDOW = 1
+RTG_VTU_AREA = 1
+RTG_VTU_SPACING = 2
 RTG_NODES_AUTO = 0
 RTG_NODES_BINARY = 2
 RTG_NODES_WIDE = 8
@@ -219,6 +221,10 @@ def load(path: str | None = None):
                                           C.POINTER(C.c_char_p), C.c_int32]),
         "rtg_read_point_cloud": (C.c_int, [C.c_char_p, _i64p, _f32p, _f32p, _f32p, C.c_char_p, C.c_int32]),
         "rtg_read_triangles": (C.c_int, [C.c_char_p, _i64p, _f32p, _i64p, _u32p, C.c_char_p, C.c_int32]),
+        "rtg_read_point_cloud_vtu": (C.c_int, [C.c_char_p, C.c_int32, _i64p, _f32p, _f32p, _f32p, C.c_char_p,
+                                               C.c_int32]),
+        "rtg_read_triangles_vtu": (C.c_int, [C.c_char_p, _i64p, _f32p, _i64p, _u32p, _f32p, C.c_char_p,
+                                             C.c_int32]),
         "rtg_set_tree_builder": (C.c_int, [_ctx, C.c_int32]),
         "rtg_get_tree_builder": (C.c_int, [_ctx, _i32p]),
         "rtg_set_node_width": (C.c_int, [_ctx, C.c_int32]),

@@ -688,4 +688,124 @@ int rtg_read_triangles(const char* path, int64_t* nv, float* vertices, int64_t* 
   return RTG_OK;
 }
 
+// rti's io/christoph and io/xaver readers: UnstructuredGrid point clouds
+// whose radius comes from an area or a grid spacing.
+int rtg_read_point_cloud_vtu(const char* path, int32_t flavor, int64_t* n, float* points, float* normals,
+                             float* radii, char* err, int32_t err_len) {
+  if (!path || !n || (flavor != RTG_VTU_AREA && flavor != RTG_VTU_SPACING)) return RTG_ERR_INVALID_ARGUMENT;
+  std::string s, e;
+  Doc doc;
+  if (!load_doc(path, s, doc, e)) return set_err(err, err_len, e), RTG_ERR_INVALID_ARGUMENT;
+  Piece& p = doc.piece;
+  DataArray* pts = find(p, "Points", nullptr);
+  if (!pts) return set_err(err, err_len, "no Points"), RTG_ERR_INVALID_ARGUMENT;
+  // christoph: point data area_around_vertex, else cell data gridSpacing; xaver: gridSpacing
+  DataArray* size = flavor == RTG_VTU_AREA ? find(p, "PointData", "area_around_vertex") : nullptr;
+  if (!size) size = find(p, "CellData", "gridSpacing");
+  DataArray* nrm = find(p, "CellData", "Normals");
+  if (!nrm) nrm = find(p, "PointData", "normal_vector");
+  if (!size)
+    return set_err(err, err_len, flavor == RTG_VTU_AREA ? "no area_around_vertex or gridSpacing data" : "no gridSpacing data"),
+           RTG_ERR_INVALID_ARGUMENT;
+  if (!nrm) return set_err(err, err_len, "no Normals or normal_vector data"), RTG_ERR_INVALID_ARGUMENT;
+  for (DataArray* d : {pts, size, nrm})
+    if (!decode(doc, s, *d, e)) return set_err(err, err_len, e), RTG_ERR_INVALID_ARGUMENT;
+  const int64_t np = (int64_t)(pts->v.size() / 3);
+  if ((int64_t)size->v.size() < np || (int64_t)nrm->v.size() < 3 * np)
+    return set_err(err, err_len, "fewer size or normal values than points"), RTG_ERR_INVALID_ARGUMENT;
+  const double grow = std::sqrt(3.0) / 2 * (1 + 1.0 / 4);  // about 25 %
+  int64_t kept = 0;
+  const bool count_only = !points && !normals && !radii;
+  for (int64_t i = 0; i < np; ++i) {
+    const double a = size->v[i];
+    const double radius = (flavor == RTG_VTU_AREA ? std::sqrt(a) : a) * grow;
+    const double* q = &nrm->v[3 * i];
+    // points of zero area (radius) or with the zero vector as normal are left out
+    if ((flavor == RTG_VTU_AREA ? a == 0 : radius == 0) || (q[0] == 0 && q[1] == 0 && q[2] == 0)) continue;
+    if (!count_only) {
+      if (kept >= *n) return set_err(err, err_len, "output arrays too small"), RTG_ERR_INVALID_ARGUMENT;
+      float c[3] = {(float)pts->v[3 * i], (float)pts->v[3 * i + 1], (float)pts->v[3 * i + 2]};
+      float u[3] = {(float)q[0], (float)q[1], (float)q[2]};
+      if (flavor == RTG_VTU_AREA) {  // the christoph reader inverts every z coordinate
+        c[2] *= -1;
+        u[2] *= -1;
+      }
+      const float len = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+      if (!(1 - 1e-6f <= len && len <= 1 + 1e-6f) && len > 0.0f)  // utils.hpp:77-93
+        for (float& x : u) x /= len;
+      if (points)
+        for (int k = 0; k < 3; ++k) points[3 * kept + k] = c[k];
+      if (normals)
+        for (int k = 0; k < 3; ++k) normals[3 * kept + k] = u[k];
+      if (radii) radii[kept] = (float)radius;
+    }
+    ++kept;
+  }
+  *n = kept;
+  return RTG_OK;
+}
+
+// rti's io/christoph/vtu_triangle_reader.hpp: every three-point cell, its
+// second and third vertex swapped, with the mean of its vertices' normals.
+int rtg_read_triangles_vtu(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices,
+                           float* normals, char* err, int32_t err_len) {
+  if (!path || !nv || !nt) return RTG_ERR_INVALID_ARGUMENT;
+  std::string s, e;
+  Doc doc;
+  if (!load_doc(path, s, doc, e)) return set_err(err, err_len, e), RTG_ERR_INVALID_ARGUMENT;
+  Piece& p = doc.piece;
+  DataArray* pts = find(p, "Points", nullptr);
+  DataArray* conn = find(p, "Cells", "connectivity");
+  DataArray* offs = find(p, "Cells", "offsets");
+  DataArray* pn = find(p, "PointData", "normal_vector");
+  if (!pts || !conn || !offs) return set_err(err, err_len, "no Points or Cells"), RTG_ERR_INVALID_ARGUMENT;
+  if (normals && !pn) return set_err(err, err_len, "no normal_vector point data"), RTG_ERR_INVALID_ARGUMENT;
+  for (DataArray* d : {pts, conn, offs})
+    if (!decode(doc, s, *d, e)) return set_err(err, err_len, e), RTG_ERR_INVALID_ARGUMENT;
+  if (pn && !decode(doc, s, *pn, e)) return set_err(err, err_len, e), RTG_ERR_INVALID_ARGUMENT;
+  const int64_t npts = (int64_t)(pts->v.size() / 3);
+  if (pn && (int64_t)pn->v.size() < 3 * npts)
+    return set_err(err, err_len, "fewer normal_vector values than points"), RTG_ERR_INVALID_ARGUMENT;
+  std::vector<uint32_t> tri;
+  double start = 0;
+  for (size_t c = 0; c < offs->v.size(); ++c) {
+    const double end = offs->v[c];
+    if (end - start == 3) {
+      uint32_t id[3];
+      for (int k = 0; k < 3; ++k) {
+        const double v = conn->v[(size_t)start + k];
+        if (!(v >= 0 && v < npts)) return set_err(err, err_len, "point index out of range"), RTG_ERR_INVALID_ARGUMENT;
+        id[k] = (uint32_t)v;
+      }
+      tri.push_back(id[0]);
+      tri.push_back(id[2]);
+      tri.push_back(id[1]);
+    }
+    start = end;
+  }
+  const int64_t ntri = (int64_t)tri.size() / 3;
+  if (!vertices && !indices && !normals) {
+    *nv = npts;
+    *nt = ntri;
+    return RTG_OK;
+  }
+  if (*nv < npts || *nt < ntri) return set_err(err, err_len, "output arrays too small"), RTG_ERR_INVALID_ARGUMENT;
+  if (vertices)
+    for (int64_t i = 0; i < 3 * npts; ++i) vertices[i] = (float)pts->v[i];
+  if (indices) std::memcpy(indices, tri.data(), tri.size() * sizeof(uint32_t));
+  if (normals)
+    for (int64_t t = 0; t < ntri; ++t) {
+      const uint32_t a = tri[3 * t], b = tri[3 * t + 2], c = tri[3 * t + 1];  // the cell's own order
+      float m[3];
+      for (int k = 0; k < 3; ++k) m[k] = (float)((pn->v[3 * a + k] + pn->v[3 * b + k] + pn->v[3 * c + k]) / 3);
+      // as the reference: every component below 1e-5 (signed) counts as no normal
+      if (m[0] < 1e-5f && m[1] < 1e-5f && m[2] < 1e-5f) m[0] = 0, m[1] = 0, m[2] = 1;
+      const float len = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+      for (int k = 0; k < 3; ++k) normals[3 * t + k] = m[k] / len;
+    }
+  *nv = npts;
+  *nt = ntri;
+  return RTG_OK;
+}
+
 }  // extern "C"

@@ -100,6 +100,41 @@ def read_triangles(path: str):
     return vx, ix
 
 
+def read_point_cloud_vtu(path: str, flavor: int = L.RTG_VTU_AREA):
+    """rti's special-purpose VTU point readers: L.RTG_VTU_AREA
+    (io/christoph: radius from area_around_vertex, z inverted) or
+    L.RTG_VTU_SPACING (io/xaver: radius from gridSpacing).  Returns the kept
+    (points, unit normals, radii) as float32."""
+    lib = L.load()
+    err = C.create_string_buffer(512)
+    n = C.c_int64(0)
+    _check_read(lib.rtg_read_point_cloud_vtu(os.fsencode(path), int(flavor), C.byref(n), None, None, None, err, 512),
+                err)
+    pts = np.zeros((n.value, 3), np.float32)
+    nrm = np.zeros((n.value, 3), np.float32)
+    rad = np.zeros(n.value, np.float32)
+    _check_read(lib.rtg_read_point_cloud_vtu(os.fsencode(path), int(flavor), C.byref(n), _p(pts, L._f32p),
+                                             _p(nrm, L._f32p), _p(rad, L._f32p), err, 512), err)
+    return pts, nrm, rad
+
+
+def read_triangles_vtu(path: str):
+    """rti's io/christoph VTU mesh reader: (vertices (nv,3), indices (nt,3) with
+    each cell's second and third vertex swapped, per-triangle mean vertex
+    normals (nt,3))."""
+    lib = L.load()
+    err = C.create_string_buffer(512)
+    nv, nt = C.c_int64(0), C.c_int64(0)
+    _check_read(lib.rtg_read_triangles_vtu(os.fsencode(path), C.byref(nv), None, C.byref(nt), None, None, err, 512),
+                err)
+    vx = np.zeros((nv.value, 3), np.float32)
+    ix = np.zeros((nt.value, 3), np.uint32)
+    nx = np.zeros((nt.value, 3), np.float32)
+    _check_read(lib.rtg_read_triangles_vtu(os.fsencode(path), C.byref(nv), _p(vx, L._f32p), C.byref(nt),
+                                           _p(ix, L._u32p), _p(nx, L._f32p), err, 512), err)
+    return vx, ix, nx
+
+
 def _check_read(rc: int, err):
     if rc != L.RTG_OK:
         raise L.RtgError(rc, err.value.decode(errors="replace"))

@@ -251,3 +251,75 @@ def test_segment_log_vtp_writer(rtg_lib, tmp_path):
     conn = np.array(lines.findall("DataArray")[0].text.split(), dtype=np.int64)
     np.testing.assert_array_equal(conn, np.arange(6))
     assert rtg_lib.rtg_write_vtp_segments(None, None, 0) == L.RTG_ERR_INVALID_ARGUMENT
+
+
+def _vtu(path, points, point_data=(), cell_data=(), cells=None):
+    """A minimal ASCII UnstructuredGrid: vertex cells unless `cells` (lists of ids) is given."""
+    def arr(name, a, ncomp):
+        vals = " ".join(repr(float(x)) for x in np.asarray(a, np.float64).ravel())
+        return (f'<DataArray type="Float64" Name="{name}" NumberOfComponents="{ncomp}" format="ascii">'
+                f'{vals}</DataArray>')
+    n = len(points)
+    cells = cells if cells is not None else [[i] for i in range(n)]
+    conn = " ".join(str(i) for c in cells for i in c)
+    offs = " ".join(str(x) for x in np.cumsum([len(c) for c in cells]))
+    types = " ".join("5" if len(c) == 3 else "1" for c in cells)
+    pd = "".join(arr(nm, a, 1 if np.ndim(a) == 1 else 3) for nm, a in point_data)
+    cd = "".join(arr(nm, a, 1 if np.ndim(a) == 1 else 3) for nm, a in cell_data)
+    path.write_text(
+        '<?xml version="1.0"?><VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian">'
+        f'<UnstructuredGrid><Piece NumberOfPoints="{n}" NumberOfCells="{len(cells)}">'
+        f'<PointData>{pd}</PointData><CellData>{cd}</CellData>'
+        f'<Points>{arr("Points", points, 3)}</Points>'
+        f'<Cells><DataArray type="Int64" Name="connectivity" format="ascii">{conn}</DataArray>'
+        f'<DataArray type="Int64" Name="offsets" format="ascii">{offs}</DataArray>'
+        f'<DataArray type="UInt8" Name="types" format="ascii">{types}</DataArray></Cells>'
+        '</Piece></UnstructuredGrid></VTKFile>')
+
+
+def test_vtu_point_cloud_readers(rtg_lib, tmp_path):
+    """rti's io/christoph and io/xaver point readers: radius rules, z inversion
+    (christoph), points with zero area / zero normal left out, normals normalised."""
+    from rti_gb300 import _lib as L
+    pts = np.array([[0.0, 0.0, 1.0], [1.0, 2.0, 3.0], [2.0, 0.5, -1.0], [3.0, 3.0, 3.0]])
+    nrm = np.array([[0.0, 0.0, 2.0], [0.0, 0.0, 0.0], [0.6, 0.0, 0.8], [1.0, 0.0, 0.0]])
+    area = np.array([0.04, 0.01, 0.09, 0.0])
+    f = tmp_path / "christoph.vtu"
+    _vtu(f, pts, point_data=[("area_around_vertex", area), ("normal_vector", nrm)])
+    p, n, r = vtk.read_point_cloud_vtu(str(f), L.RTG_VTU_AREA)
+    grow = np.sqrt(3.0) / 2 * 1.25
+    keep = [0, 2]  # point 1 has the zero normal, point 3 zero area
+    np.testing.assert_array_equal(p, (pts[keep] * [1, 1, -1]).astype(np.float32))
+    np.testing.assert_allclose(n, [[0, 0, -1], [0.6, 0, -0.8]], atol=1e-7)
+    np.testing.assert_allclose(r, np.sqrt(area[keep]) * grow, rtol=1e-6)
+    # the christoph reader falls back to a gridSpacing cell array (still through the square root)
+    g = tmp_path / "spacing.vtu"
+    spacing = np.array([0.02, 0.02, 0.0, 0.05])
+    _vtu(g, pts, point_data=[("normal_vector", nrm)], cell_data=[("gridSpacing", spacing)])
+    _, _, r2 = vtk.read_point_cloud_vtu(str(g), L.RTG_VTU_AREA)
+    np.testing.assert_allclose(r2, np.sqrt([0.02, 0.05]) * grow, rtol=1e-6)
+    # xaver: gridSpacing itself, z kept
+    p3, n3, r3 = vtk.read_point_cloud_vtu(str(g), L.RTG_VTU_SPACING)
+    np.testing.assert_array_equal(p3, pts[[0, 3]].astype(np.float32))
+    np.testing.assert_allclose(r3, np.array([0.02, 0.05]) * grow, rtol=1e-6)
+    np.testing.assert_allclose(n3, [[0, 0, 1], [1, 0, 0]], atol=1e-7)
+    with pytest.raises(RtgError, match="gridSpacing"):
+        vtk.read_point_cloud_vtu(str(f), L.RTG_VTU_SPACING)
+
+
+def test_vtu_triangle_reader(rtg_lib, tmp_path):
+    """rti's io/christoph mesh reader: three-point cells with the second and
+    third vertex swapped, mean vertex normals normalised, (0, 0, 1) where all
+    three mean components are below 1e-5 (signed, as the reference)."""
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]], np.float64)
+    vn = np.array([[0, 0, 2], [0, 0, 1], [0, 0, 1], [-1, 0, 0]], np.float64)
+    cells = [[0, 1, 2], [1, 3, 2], [0, 3], [3, 3, 3]]
+    f = tmp_path / "mesh.vtu"
+    _vtu(f, v, point_data=[("normal_vector", vn)], cells=cells)
+    vx, ix, nx = vtk.read_triangles_vtu(str(f))
+    np.testing.assert_array_equal(vx, v.astype(np.float32))
+    np.testing.assert_array_equal(ix, [[0, 2, 1], [1, 2, 3], [3, 3, 3]])
+    np.testing.assert_allclose(nx[0], [0, 0, 1], atol=1e-7)
+    m = (vn[1] + vn[3] + vn[2]) / 3
+    np.testing.assert_allclose(nx[1], m / np.linalg.norm(m), atol=1e-6)
+    np.testing.assert_allclose(nx[2], [0, 0, 1])  # mean (-1, 0, 0): every component below 1e-5
