@@ -474,7 +474,13 @@ void rtg_config_default(rtg_config* c) {
   c->job = 0;
 }
 
+static int rtg_create_body(rtg_context** out, int device);
+
 int rtg_create(rtg_context** out, int device) {
+  return rtg::host_guard(nullptr, [&] { return rtg_create_body(out, device); });
+}
+
+static int rtg_create_body(rtg_context** out, int device) {
   if (!out) return RTG_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   int ndev = 0;
@@ -603,7 +609,13 @@ int rtg_update_discs(rtg_context* ctx, const float* points, const float* normals
   return RTG_OK;
 }
 
+static int rtg_update_vertices_body(rtg_context* ctx, const float* vertices, int64_t nv);
+
 int rtg_update_vertices(rtg_context* ctx, const float* vertices, int64_t nv) {
+  return rtg::host_guard(ctx, [&] { return rtg_update_vertices_body(ctx, vertices, nv); });
+}
+
+static int rtg_update_vertices_body(rtg_context* ctx, const float* vertices, int64_t nv) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   Geometry& g = ctx->g;
   if (g.nt == 0 || nv != g.nv || !vertices)
@@ -845,7 +857,15 @@ int rtg_get_deposit_mode(const rtg_context* ctx, int32_t* mode, float* window_fa
   return RTG_OK;
 }
 
+static int rtg_autotune_body(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
+                 double* best_rays_per_s);
+
 int rtg_autotune(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
+                 double* best_rays_per_s) {
+  return rtg::host_guard(ctx, [&] { return rtg_autotune_body(ctx, sample_rays, seed, best, best_rays_per_s); });
+}
+
+static int rtg_autotune_body(rtg_context* ctx, uint64_t sample_rays, uint64_t seed, rtg_launch_config* best,
                  double* best_rays_per_s) {
   if (!ctx || sample_rays == 0) return RTG_ERR_INVALID_ARGUMENT;
   TraceParams p{};
@@ -1034,7 +1054,13 @@ static int read_segment_log(rtg_context* ctx, std::vector<rtg_segment>& out, uin
   return RTG_OK;
 }
 
+static int rtg_get_segment_log_body(rtg_context* ctx, rtg_segment* out, uint64_t cap, uint64_t* n_kept, uint64_t* n_dropped);
+
 int rtg_get_segment_log(rtg_context* ctx, rtg_segment* out, uint64_t cap, uint64_t* n_kept, uint64_t* n_dropped) {
+  return rtg::host_guard(ctx, [&] { return rtg_get_segment_log_body(ctx, out, cap, n_kept, n_dropped); });
+}
+
+static int rtg_get_segment_log_body(rtg_context* ctx, rtg_segment* out, uint64_t cap, uint64_t* n_kept, uint64_t* n_dropped) {
   if (!ctx || (cap > 0 && !out)) return RTG_ERR_INVALID_ARGUMENT;
   std::vector<rtg_segment> v;
   uint64_t dropped = 0;
@@ -1045,7 +1071,13 @@ int rtg_get_segment_log(rtg_context* ctx, rtg_segment* out, uint64_t cap, uint64
   return RTG_OK;
 }
 
+static int rtg_write_segment_log_vtp_body(rtg_context* ctx, const char* path);
+
 int rtg_write_segment_log_vtp(rtg_context* ctx, const char* path) {
+  return rtg::host_guard(ctx, [&] { return rtg_write_segment_log_vtp_body(ctx, path); });
+}
+
+static int rtg_write_segment_log_vtp_body(rtg_context* ctx, const char* path) {
   if (!ctx || !path) return RTG_ERR_INVALID_ARGUMENT;
   if (!ctx->seglog.p) return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "no segment log (rtg_set_segment_log)");
   std::vector<rtg_segment> v;
@@ -1323,7 +1355,15 @@ int rtg_get_device_view(rtg_context* ctx, rtg_device_view* v) {
   return RTG_OK;
 }
 
+static int rtg_write_vtp_body(rtg_context* ctx, const char* path, const char* const* meta_keys, const char* const* meta_values,
+                  int32_t n_meta);
+
 int rtg_write_vtp(rtg_context* ctx, const char* path, const char* const* meta_keys, const char* const* meta_values,
+                  int32_t n_meta) {
+  return rtg::host_guard(ctx, [&] { return rtg_write_vtp_body(ctx, path, meta_keys, meta_values, n_meta); });
+}
+
+static int rtg_write_vtp_body(rtg_context* ctx, const char* path, const char* const* meta_keys, const char* const* meta_values,
                   int32_t n_meta) {
   if (!ctx || !path || (n_meta > 0 && (!meta_keys || !meta_values))) return RTG_ERR_INVALID_ARGUMENT;
   if (!ctx->traced) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "write_vtp: no trace results yet");
@@ -1364,7 +1404,17 @@ int rtg_write_vtp(rtg_context* ctx, const char* path, const char* const* meta_ke
   return RTG_OK;
 }
 
+static int rtg_device_run_body(const float* points, const float* normals, const float* radii, int64_t n, const rtg_config* cfg,
+                   const float* sticking_field, uint64_t n_rays, uint64_t seed, float* est_out, uint64_t* cnt_out,
+                   int device);
+
 int rtg_device_run(const float* points, const float* normals, const float* radii, int64_t n, const rtg_config* cfg,
+                   const float* sticking_field, uint64_t n_rays, uint64_t seed, float* est_out, uint64_t* cnt_out,
+                   int device) {
+  return rtg::host_guard(nullptr, [&] { return rtg_device_run_body(points, normals, radii, n, cfg, sticking_field, n_rays, seed, est_out, cnt_out, device); });
+}
+
+static int rtg_device_run_body(const float* points, const float* normals, const float* radii, int64_t n, const rtg_config* cfg,
                    const float* sticking_field, uint64_t n_rays, uint64_t seed, float* est_out, uint64_t* cnt_out,
                    int device) {
   rtg_context* ctx = nullptr;

@@ -165,7 +165,13 @@ int refresh_jobs(rtg_batch* b) {
 
 extern "C" {
 
+static int rtg_batch_create_body(rtg_batch** out, int device);
+
 int rtg_batch_create(rtg_batch** out, int device) {
+  return rtg::host_guard(nullptr, [&] { return rtg_batch_create_body(out, device); });
+}
+
+static int rtg_batch_create_body(rtg_batch** out, int device) {
   if (!out) return RTG_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   int ndev = 0;
@@ -214,7 +220,15 @@ int rtg_batch_destroy(rtg_batch* b) {
 
 const char* rtg_batch_last_error(const rtg_batch* b) { return b ? b->aux.err.c_str() : "null batch"; }
 
+static int rtg_batch_add_body(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint64_t n_rays, uint64_t seed,
+                  int32_t* job_out);
+
 int rtg_batch_add(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint64_t n_rays, uint64_t seed,
+                  int32_t* job_out) {
+  return rtg::host_guard(b ? &b->aux : nullptr, [&] { return rtg_batch_add_body(b, scene, cfg, n_rays, seed, job_out); });
+}
+
+static int rtg_batch_add_body(rtg_batch* b, rtg_context* scene, const rtg_config* cfg, uint64_t n_rays, uint64_t seed,
                   int32_t* job_out) {
   if (!b || !scene) return RTG_ERR_INVALID_ARGUMENT;
   rtg_context* ctx = &b->aux;
@@ -289,7 +303,13 @@ int rtg_batch_run(rtg_batch* b, int use_graph, void* stream) {
   return RTG_OK;
 }
 
+static int rtg_batch_run_sequential_body(rtg_batch* b, void* stream);
+
 int rtg_batch_run_sequential(rtg_batch* b, void* stream) {
+  return rtg::host_guard(b ? &b->aux : nullptr, [&] { return rtg_batch_run_sequential_body(b, stream); });
+}
+
+static int rtg_batch_run_sequential_body(rtg_batch* b, void* stream) {
   if (!b) return RTG_ERR_INVALID_ARGUMENT;
   rtg_context* ctx = &b->aux;
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -376,7 +396,13 @@ int rtg_batch_get_launch_config(const rtg_batch* b, rtg_launch_config* lc) {
   return RTG_OK;
 }
 
+static int rtg_batch_autotune_body(rtg_batch* b, double fraction, rtg_launch_config* best, double* best_rays_per_s);
+
 int rtg_batch_autotune(rtg_batch* b, double fraction, rtg_launch_config* best, double* best_rays_per_s) {
+  return rtg::host_guard(b ? &b->aux : nullptr, [&] { return rtg_batch_autotune_body(b, fraction, best, best_rays_per_s); });
+}
+
+static int rtg_batch_autotune_body(rtg_batch* b, double fraction, rtg_launch_config* best, double* best_rays_per_s) {
   if (!b || !(fraction > 0.0 && fraction <= 1.0)) return RTG_ERR_INVALID_ARGUMENT;
   rtg_context* ctx = &b->aux;
   RTG_CUDA(ctx, cudaSetDevice(ctx->device));

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <new>
 #include <string>
 
 #include <nvtx3/nvToolsExt.h>
@@ -314,6 +315,28 @@ int prepare_trace_with(rtg_context* ctx, const rtg_config& c, const float* box_l
                        uint64_t ray_begin, uint64_t ray_end, uint64_t seed, TraceParams& p);
 int set_error(rtg_context* ctx, int code, const std::string& msg);
 int check_cuda(rtg_context* ctx, cudaError_t e, const char* what);
+// Runs an entry point's body and turns a C++ exception (a failed host
+// allocation, above all) into an error code, so that none crosses the C ABI.
+template <typename F>
+int host_guard(rtg_context* ctx, F&& f) noexcept {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    if (!ctx) return RTG_ERR_OUT_OF_MEMORY;
+    try {
+      return set_error(ctx, RTG_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (...) {
+      return RTG_ERR_OUT_OF_MEMORY;
+    }
+  } catch (...) {
+    if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+    try {
+      return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "unexpected host exception");
+    } catch (...) {
+      return RTG_ERR_INVALID_ARGUMENT;
+    }
+  }
+}
 // Fault injection (rtg_inject_alloc_failure): whether this allocation is the
 // one chosen to fail.
 inline bool injected_alloc_failure(rtg_context* ctx) {

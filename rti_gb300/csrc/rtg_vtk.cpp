@@ -25,6 +25,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <new>
+#include <stdexcept>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -398,13 +400,15 @@ bool inflate_blocks(const std::vector<unsigned char>& header, const unsigned cha
 #ifdef RTG_HAVE_ZLIB
   const uint64_t nb = header_word(header, 0, hs, swap), bs = header_word(header, 1, hs, swap);
   const uint64_t last = header_word(header, 2, hs, swap);
-  if (header.size() < (3 + nb) * hs) return err = "truncated compression header", false;
+  if (nb > header.size() / hs || header.size() / hs - nb < 3) return err = "truncated compression header", false;
   out.clear();
   size_t pos = 0;
   for (uint64_t b = 0; b < nb; ++b) {
     const uint64_t cs = header_word(header, 3 + b, hs, swap);
     const uint64_t us = (b + 1 == nb && last != 0) ? last : bs;
-    if (pos + cs > avail) return err = "truncated compressed block", false;
+    if (cs > avail - pos) return err = "truncated compressed block", false;
+    // zlib expands at most about 1032:1, so a larger size is a damaged header
+    if (us > 1100 * cs + 64) return err = "compressed block larger than zlib allows", false;
     const size_t o0 = out.size();
     out.resize(o0 + us);
     uLongf dl = (uLongf)us;
@@ -448,6 +452,7 @@ bool decode(const Doc& doc, const std::string& s, DataArray& d, std::string& err
       n = d.text.size();
     } else {
       if (d.offset < 0 || doc.appended_start == std::string::npos) return err = "appended array without offset", false;
+      if ((size_t)d.offset > s.size() - doc.appended_start) return err = "appended data out of range", false;
       p = s.c_str() + doc.appended_start + (size_t)d.offset;
       n = s.size() - doc.appended_start - (size_t)d.offset;
     }
@@ -470,9 +475,11 @@ bool decode(const Doc& doc, const std::string& s, DataArray& d, std::string& err
       // compression header in its own base64 run, then the compressed blocks
       const size_t h3 = (3 * hs + 2) / 3 * 4;
       std::vector<unsigned char> h = b64(p, std::min(n, h3));
-      if (h.size() < 3 * hs) return err = "truncated compression header", false;
+      if (h.size() < 3 * hs || n < h3) return err = "truncated compression header", false;
       const uint64_t nb = header_word(h, 0, hs, swap);
+      if (nb > (n - h3) / hs) return err = "truncated compression header", false;
       const size_t hb = (nb * hs + 2) / 3 * 4;
+      if (hb > n - h3) return err = "truncated compression header", false;
       std::vector<unsigned char> sizes = b64(p + h3, std::min(n - h3, hb));
       h.insert(h.end(), sizes.begin(), sizes.end());
       std::vector<unsigned char> data = b64(p + h3 + hb, n - h3 - hb);
@@ -487,13 +494,13 @@ bool decode(const Doc& doc, const std::string& s, DataArray& d, std::string& err
     if (!zl) {
       std::vector<unsigned char> h(p, p + hs);
       const uint64_t nbytes = header_word(h, 0, hs, swap);
-      if (hs + nbytes > avail) return err = "appended data out of range", false;
+      if (nbytes > avail - hs) return err = "appended data out of range", false;
       bytes.assign(p + hs, p + hs + nbytes);
     } else {
       std::vector<unsigned char> h(p, p + std::min(avail, 3 * hs));
       if (h.size() < 3 * hs) return err = "truncated compression header", false;
       const uint64_t nb = header_word(h, 0, hs, swap);
-      if ((3 + nb) * hs > avail) return err = "truncated compression header", false;
+      if (nb > avail / hs - 3) return err = "truncated compression header", false;
       h.assign(p, p + (3 + nb) * hs);
       if (!inflate_blocks(h, p + (3 + nb) * hs, avail - (3 + nb) * hs, hs, swap, bytes, err)) return false;
     }
@@ -524,6 +531,24 @@ DataArray* find(Piece& p, const char* section, const char* name) {
 void set_err(char* buf, int32_t len, const std::string& m) {
   if (buf && len > 0) {
     std::snprintf(buf, (size_t)len, "%s", m.c_str());
+  }
+}
+
+// The readers' vectors grow with the file; a host allocation that fails (or
+// any other exception) becomes an error code instead of crossing the C ABI.
+template <typename F>
+int guarded(char* err, int32_t err_len, F&& f) noexcept {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    set_err(err, err_len, "out of host memory");
+    return RTG_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return RTG_ERR_INVALID_ARGUMENT;
+  } catch (...) {
+    set_err(err, err_len, "unexpected error");
+    return RTG_ERR_INVALID_ARGUMENT;
   }
 }
 
@@ -597,7 +622,7 @@ int rtg_write_vtp_mixed(const char* path, int64_t nd, const float* points, const
                         n_meta);
 }
 
-int rtg_read_point_cloud(const char* path, int64_t* n, float* points, float* normals, float* radii, char* err,
+static int rtg_read_point_cloud_impl(const char* path, int64_t* n, float* points, float* normals, float* radii, char* err,
                          int32_t err_len) {
   if (!path || !n) return RTG_ERR_INVALID_ARGUMENT;
   std::string s, e;
@@ -640,7 +665,7 @@ int rtg_read_point_cloud(const char* path, int64_t* n, float* points, float* nor
   return RTG_OK;
 }
 
-int rtg_read_triangles(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices, char* err,
+static int rtg_read_triangles_impl(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices, char* err,
                        int32_t err_len) {
   if (!path || !nv || !nt) return RTG_ERR_INVALID_ARGUMENT;
   std::string s, e;
@@ -663,6 +688,8 @@ int rtg_read_triangles(const char* path, int64_t* nv, float* vertices, int64_t* 
   double start = 0;
   for (size_t c = 0; c < offs->v.size(); ++c) {
     const double end = offs->v[c];
+    if (!(end >= start && end <= (double)conn->v.size()))
+      return set_err(err, err_len, "cell offsets out of range"), RTG_ERR_INVALID_ARGUMENT;
     const bool is_tri = end - start == 3 && (!types || (c < types->v.size() && types->v[c] == 5));
     if (is_tri) {  // vtp_triangle_reader.hpp:56-63: three-point cells only
       for (int k = 0; k < 3; ++k) {
@@ -690,7 +717,7 @@ int rtg_read_triangles(const char* path, int64_t* nv, float* vertices, int64_t* 
 
 // rti's io/christoph and io/xaver readers: UnstructuredGrid point clouds
 // whose radius comes from an area or a grid spacing.
-int rtg_read_point_cloud_vtu(const char* path, int32_t flavor, int64_t* n, float* points, float* normals,
+static int rtg_read_point_cloud_vtu_impl(const char* path, int32_t flavor, int64_t* n, float* points, float* normals,
                              float* radii, char* err, int32_t err_len) {
   if (!path || !n || (flavor != RTG_VTU_AREA && flavor != RTG_VTU_SPACING)) return RTG_ERR_INVALID_ARGUMENT;
   std::string s, e;
@@ -747,7 +774,7 @@ int rtg_read_point_cloud_vtu(const char* path, int32_t flavor, int64_t* n, float
 
 // rti's io/christoph/vtu_triangle_reader.hpp: every three-point cell, its
 // second and third vertex swapped, with the mean of its vertices' normals.
-int rtg_read_triangles_vtu(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices,
+static int rtg_read_triangles_vtu_impl(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices,
                            float* normals, char* err, int32_t err_len) {
   if (!path || !nv || !nt) return RTG_ERR_INVALID_ARGUMENT;
   std::string s, e;
@@ -770,6 +797,8 @@ int rtg_read_triangles_vtu(const char* path, int64_t* nv, float* vertices, int64
   double start = 0;
   for (size_t c = 0; c < offs->v.size(); ++c) {
     const double end = offs->v[c];
+    if (!(end >= start && end <= (double)conn->v.size()))
+      return set_err(err, err_len, "cell offsets out of range"), RTG_ERR_INVALID_ARGUMENT;
     if (end - start == 3) {
       uint32_t id[3];
       for (int k = 0; k < 3; ++k) {
@@ -806,6 +835,26 @@ int rtg_read_triangles_vtu(const char* path, int64_t* nv, float* vertices, int64
   *nv = npts;
   *nt = ntri;
   return RTG_OK;
+}
+
+int rtg_read_point_cloud(const char* path, int64_t* n, float* points, float* normals, float* radii, char* err,
+                         int32_t err_len) {
+  return guarded(err, err_len, [&] { return rtg_read_point_cloud_impl(path, n, points, normals, radii, err, err_len); });
+}
+
+int rtg_read_triangles(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices, char* err,
+                       int32_t err_len) {
+  return guarded(err, err_len, [&] { return rtg_read_triangles_impl(path, nv, vertices, nt, indices, err, err_len); });
+}
+
+int rtg_read_point_cloud_vtu(const char* path, int32_t flavor, int64_t* n, float* points, float* normals,
+                             float* radii, char* err, int32_t err_len) {
+  return guarded(err, err_len, [&] { return rtg_read_point_cloud_vtu_impl(path, flavor, n, points, normals, radii, err, err_len); });
+}
+
+int rtg_read_triangles_vtu(const char* path, int64_t* nv, float* vertices, int64_t* nt, uint32_t* indices,
+                           float* normals, char* err, int32_t err_len) {
+  return guarded(err, err_len, [&] { return rtg_read_triangles_vtu_impl(path, nv, vertices, nt, indices, normals, err, err_len); });
 }
 
 }  // extern "C"

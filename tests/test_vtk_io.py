@@ -207,6 +207,12 @@ def test_unstructured_triangles_skip_other_cells(tmp_path):
     v2, t2 = vtk.read_triangles(str(f))
     np.testing.assert_array_equal(v2, v)
     np.testing.assert_array_equal(t2, [[0, 1, 2], [1, 2, 7]])
+    # an offset past the connectivity array is refused, not read
+    g = tmp_path / "u_bad.vtu"
+    arrays[2] = ("Cells", "offsets", np.array([3, 7, 13], np.int64), 1)
+    _write_encoded(g, arrays, "raw", "UInt64", False, unstructured=True, cells=3)
+    with pytest.raises(RtgError, match="offsets"):
+        vtk.read_triangles(str(g))
 
 
 def test_reader_errors(tmp_path):
@@ -323,3 +329,10 @@ def test_vtu_triangle_reader(rtg_lib, tmp_path):
     m = (vn[1] + vn[3] + vn[2]) / 3
     np.testing.assert_allclose(nx[1], m / np.linalg.norm(m), atol=1e-6)
     np.testing.assert_allclose(nx[2], [0, 0, 1])  # mean (-1, 0, 0): every component below 1e-5
+    # offsets past the connectivity array are refused, not read
+    bad = tmp_path / "bad.vtu"
+    bad.write_text(f.read_text().replace('Name="offsets" format="ascii">3 6 8 11<',
+                                         'Name="offsets" format="ascii">3 6 8 14<'))
+    assert bad.read_text() != f.read_text()
+    with pytest.raises(RtgError, match="offsets"):
+        vtk.read_triangles_vtu(str(bad))
