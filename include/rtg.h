@@ -337,6 +337,18 @@ RTG_API int rtg_get_exposed_areas(rtg_context* ctx, float* out);
 RTG_API int rtg_get_relative_error(rtg_context* ctx, double* out);
 RTG_API int rtg_get_vov(rtg_context* ctx, double* out);
 RTG_API int rtg_get_tally(rtg_context* ctx, rtg_tally* out);
+/* Checkpoint and resume (no counterpart in rti, whose trace is one OpenMP
+ * loop; the state of hit_accumulator.hpp:271-290 plus result.hpp's counts):
+ * rtg_get_accumulators, rtg_get_hit_counts and rtg_get_tally save a trace of
+ * the ray range [0, k); rtg_set_accumulators puts that state back into a
+ * context holding the same surface and configuration, and
+ * rtg_trace_range(ctx, k, n, seed, 1, stream) continues it.  Paths depend only
+ * on (seed, ray id), so the result equals the trace of [0, n) in one go: the
+ * same hit counts and tallies, S1 bit for bit under RTG_ACCUM_FIXED (S2..S4
+ * and plain S1 up to the order of the FP64 additions).  All five arrays hold
+ * rtg_num_primitives values; the tally's timings are ignored. */
+RTG_API int rtg_set_accumulators(rtg_context* ctx, const double* s1, const double* s2, const double* s3,
+                                 const double* s4, const uint64_t* counts, const rtg_tally* tally);
 /* Neighbour CSR of the discs: row_ptr (nd+1), cols (cap entries); *nnz gets the count. */
 RTG_API int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols, int64_t cap, int64_t* nnz);
 

@@ -35,7 +35,7 @@ EXPORTS = [
     "rtg_set_config", "rtg_get_config", "rtg_get_box", "rtg_set_sticking", "rtg_set_sticking_field",
     "rtg_trace", "rtg_trace_range", "rtg_synchronize", "rtg_request_abort", "rtg_trace_rays",
     "rtg_num_primitives", "rtg_get_mc_estimates", "rtg_get_hit_counts", "rtg_get_accumulators",
-    "rtg_get_exposed_areas", "rtg_get_relative_error", "rtg_get_vov", "rtg_get_tally",
+    "rtg_get_exposed_areas", "rtg_get_relative_error", "rtg_get_vov", "rtg_get_tally", "rtg_set_accumulators",
     "rtg_get_neighbors", "rtg_get_device_view", "rtg_device_run", "rtg_get_mc_estimates_noalloc",
     "rtg_set_sticking_field_device", "rtg_adjoint", "rtg_adjoint_host",
     "rtg_batch_create", "rtg_batch_destroy", "rtg_batch_last_error", "rtg_batch_add", "rtg_batch_num_jobs",
@@ -188,6 +188,7 @@ def load(path: str | None = None):
         "rtg_get_relative_error": (C.c_int, [_ctx, _f64p]),
         "rtg_get_vov": (C.c_int, [_ctx, _f64p]),
         "rtg_get_tally": (C.c_int, [_ctx, C.POINTER(RtgTally)]),
+        "rtg_set_accumulators": (C.c_int, [_ctx, _f64p, _f64p, _f64p, _f64p, _u64p, C.POINTER(RtgTally)]),
         "rtg_get_neighbors": (C.c_int, [_ctx, _i64p, _i32p, C.c_int64, _i64p]),
         "rtg_get_device_view": (C.c_int, [_ctx, C.POINTER(RtgDeviceView)]),
         "rtg_device_run": (C.c_int, [_f32p, _f32p, _f32p, C.c_int64, C.POINTER(RtgConfig), _f32p, C.c_uint64,

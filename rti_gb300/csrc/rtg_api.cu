@@ -1326,6 +1326,43 @@ int rtg_get_tally(rtg_context* ctx, rtg_tally* out) {
   return RTG_OK;
 }
 
+int rtg_set_accumulators(rtg_context* ctx, const double* s1, const double* s2, const double* s3, const double* s4,
+                         const uint64_t* counts, const rtg_tally* tally) {
+  if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
+  if (!s1 || !s2 || !s3 || !s4 || !counts || !tally)
+    return set_error(ctx, RTG_ERR_INVALID_ARGUMENT, "set_accumulators: S1..S4, counts and tally are all needed");
+  const int64_t np = ctx->g.nd + ctx->g.nt;
+  if (np == 0 || !ctx->acc.p || !ctx->cnt.p) return set_error(ctx, RTG_ERR_NO_GEOMETRY, "no geometry uploaded");
+  RTG_TRY(use_device(ctx));
+  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  RTG_CUDA(ctx, cudaDeviceSynchronize());  // no trace of this context may still write the accumulators
+  const size_t bytes = (size_t)np * sizeof(double);
+  const double* s[4] = {s1, s2, s3, s4};
+  for (int k = 0; k < 4; ++k)
+    RTG_CUDA(ctx, cudaMemcpy(ctx->acc.p + (size_t)k * np, s[k], bytes, cudaMemcpyHostToDevice));
+  RTG_CUDA(ctx, cudaMemcpy(ctx->cnt.p, counts, (size_t)np * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+  DevTally t{};
+  t.hitc = tally->hitc;
+  t.nonhitc = tally->nonhitc;
+  t.total = tally->total;
+  t.segments = tally->segments;
+  t.truncated = tally->truncated;
+  t.nb_deposits = tally->nb_deposits;
+  t.errors = tally->errors;
+  RTG_CUDA(ctx, cudaMemcpy(ctx->d_tally, &t, sizeof t, cudaMemcpyHostToDevice));
+  // the exposed areas of this surface, and zero-length timings for the getters
+  RTG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  RTG_CUDA(ctx, cudaEventRecord(ctx->evk0, ctx->stream));
+  RTG_CUDA(ctx, cudaEventRecord(ctx->evk1, ctx->stream));
+  RTG_TRY(compute_areas(ctx, ctx->stream, ctx->box_lo, ctx->box_hi));
+  RTG_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  RTG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->last_rays = tally->num_rays;
+  ctx->traced = true;
+  ctx->finalized = false;
+  return RTG_OK;
+}
+
 int rtg_get_neighbors(rtg_context* ctx, int64_t* row_ptr, int32_t* cols, int64_t cap, int64_t* nnz) {
   if (!ctx) return RTG_ERR_INVALID_ARGUMENT;
   RTG_TRY(use_device(ctx));

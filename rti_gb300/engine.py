@@ -379,6 +379,30 @@ class Engine:
         self._check(self._L.rtg_get_vov(self._h, _ptr(out, L._f64p)))
         return out
 
+    def checkpoint(self) -> dict:
+        """The state of the trace so far (S1..S4, hit counts, tally): with
+        resume() on a context holding the same surface and configuration, a
+        trace of the remaining rays (trace(..., ray_begin=k, accumulate=True))
+        continues it as if it had not stopped."""
+        s1, s2, s3, s4 = self.accumulators()
+        t = self.tally()
+        return {"s1": s1, "s2": s2, "s3": s3, "s4": s4, "counts": self.hit_counts().copy(),
+                "tally": {f: getattr(t, f) for f in ("num_rays", "hitc", "nonhitc", "total", "segments",
+                                                     "truncated", "nb_deposits", "errors")}}
+
+    def resume(self, state: dict):
+        """Puts a checkpoint() back (rtg_set_accumulators)."""
+        n = self.num_primitives
+        arrs = [np.ascontiguousarray(state[k], dtype=np.float64) for k in ("s1", "s2", "s3", "s4")]
+        cnt = np.ascontiguousarray(state["counts"], dtype=np.uint64)
+        if any(a.shape != (n,) for a in arrs) or cnt.shape != (n,):
+            raise ValueError(f"checkpoint arrays must hold {n} values")
+        t = L.RtgTally()
+        for f, v in state["tally"].items():
+            setattr(t, f, int(v))
+        self._check(self._L.rtg_set_accumulators(self._h, *[_ptr(a, L._f64p) for a in arrs], _ptr(cnt, L._u64p),
+                                                 C.byref(t)))
+
     def tally(self) -> Tally:
         t = L.RtgTally()
         self._check(self._L.rtg_get_tally(self._h, C.byref(t)))
