@@ -106,3 +106,44 @@ def test_random_surface_and_configuration(eng, oracle_lib, k):
         assert np.array_equal(s1.view(np.uint64), ref.s1.view(np.uint64))
     else:
         np.testing.assert_allclose(s1, ref.s1, rtol=1e-9, atol=0)
+
+
+ADJ_CASES = 24
+
+
+@pytest.mark.parametrize("k", range(ADJ_CASES))
+def test_random_adjoint(eng, oracle_lib, k):
+    """The adjoint replay on the same random surfaces (with the neighbour
+    deposit): dL/ds, dL/dn and, with a sticking field, dL/ds_j for random
+    weights g, held or unbiased estimator, to the order of the FP64 sums."""
+    c = _case(k)
+    lo, hi = c["box"]
+    rng = np.random.default_rng(9000 + k)
+    unbiased = bool(rng.random() < 0.5)
+    eng.set_node_width(c["width"])
+    if c["kind"] == "discs":
+        eng.upload_discs(c["points"], c["normals"], c["radii"])
+    elif c["kind"] == "triangles":
+        eng.upload_triangles(c["vertices"], c["indices"])
+    else:
+        eng.upload_mixed(c["points"], c["normals"], c["radii"], c["vertices"], c["indices"])
+    eng.configure(box=(lo, hi), reset=True, **c["cfg"])
+    eng.set_sticking_field(c["field"])
+    g = rng.random(eng.num_primitives)
+    try:
+        ds, dn, fg = eng.adjoint(g, N_RAYS, seed=c["seed"], unbiased=unbiased)
+    finally:
+        eng.set_node_width(0)
+        eng.set_sticking_field(None)
+    xyzr = (np.concatenate([c["points"], c["radii"][:, None]], 1) if "points" in c else None)
+    s = oracle_lib.Scene(xyzr, c.get("normals"), c.get("vertices"), c.get("indices"))
+    if s.nd:
+        s.neighbors(bruteforce=True)
+    cfg = oracle_lib.make_config(lo, hi, seed=c["seed"], **c["cfg"])
+    ods, odn, ofg, _ = oracle_lib.adjoint(s, cfg, g, 0, N_RAYS, sticking_field=c["field"], unbiased=unbiased)
+    assert abs(dn - odn) <= 1e-9 * abs(odn) + 1e-12
+    if c["field"] is None:
+        assert abs(ds - ods) <= 1e-9 * abs(ods) + 1e-12
+    else:
+        assert ds == 0.0
+        np.testing.assert_allclose(fg, ofg, rtol=1e-9, atol=1e-9 * np.abs(ofg).max())
