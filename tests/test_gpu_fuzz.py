@@ -147,3 +147,49 @@ def test_random_adjoint(eng, oracle_lib, k):
     else:
         assert ds == 0.0
         np.testing.assert_allclose(fg, ofg, rtol=1e-9, atol=1e-9 * np.abs(ofg).max())
+
+
+BATCH_JOBS = 12
+
+
+def test_random_batch(rtg_lib, oracle_lib):
+    """One batched launch (CUDA graph) over 12 of the random surfaces, each
+    with its own configuration, sticking field and tree width; lanes of a warp
+    carry paths of different jobs.  Every job equals the oracle's trace with
+    the job's Philox tag."""
+    from rti_gb300 import Engine
+    from rti_gb300.batch import Batch
+    cases = [_case(k) for k in range(BATCH_JOBS)]
+    engines = []
+    try:
+        for c in cases:
+            e = Engine(0)
+            engines.append(e)
+            e.set_node_width(c["width"])
+            if c["kind"] == "discs":
+                e.upload_discs(c["points"], c["normals"], c["radii"])
+            elif c["kind"] == "triangles":
+                e.upload_triangles(c["vertices"], c["indices"])
+            else:
+                e.upload_mixed(c["points"], c["normals"], c["radii"], c["vertices"], c["indices"])
+            e.configure(box=c["box"], reset=True, **c["cfg"])
+            e.set_sticking_field(c["field"])
+        with Batch(0) as b:
+            jobs = [b.add(e, N_RAYS + 100 * i, seed=c["seed"]) for i, (e, c) in enumerate(zip(engines, cases))]
+            b.run(use_graph=True)
+            b.synchronize()
+            assert b.tally().errors == 0
+            got = [b.results(j) for j in jobs]
+    finally:
+        for e in engines:
+            e.close()
+    for i, (c, j, (s1, cnt, _)) in enumerate(zip(cases, jobs, got)):
+        lo, hi = c["box"]
+        xyzr = (np.concatenate([c["points"], c["radii"][:, None]], 1) if "points" in c else None)
+        s = oracle_lib.Scene(xyzr, c.get("normals"), c.get("vertices"), c.get("indices"))
+        if s.nd:
+            s.neighbors(bruteforce=True)
+        cfg = oracle_lib.make_config(lo, hi, seed=c["seed"], job=j, **c["cfg"])
+        ref = s.trace(cfg, 0, N_RAYS + 100 * i, sticking_field=c["field"])
+        assert np.array_equal(cnt, ref.counts), i
+        np.testing.assert_allclose(s1, ref.s1, rtol=1e-9, atol=0)
