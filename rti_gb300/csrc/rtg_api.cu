@@ -91,7 +91,7 @@ namespace {
 void resolve_box(rtg_context* ctx) { box_for(ctx->cfg, ctx->g, ctx->box_lo, ctx->box_hi); }
 
 // ---- upload: the host arrays are copied as they are and checked and
-// converted on the device; one small read-back carries the verdict ----
+// converted on the device; one small read-back carries the outcome ----
 
 // Bounds and first offending index of an upload.
 struct UploadCheck {
@@ -237,7 +237,7 @@ void check_reset(UploadCheck& h) {
   h.bad_tri = ~0ull;
 }
 
-// Copies n discs to the device, converts and checks them; the verdict is
+// Copies n discs to the device, converts and checks them; the outcome is
 // read back (one synchronisation).  Leaves the context untouched.
 int stage_discs(rtg_context* ctx, const float* pts, const float* nrm, const float* rad, int64_t n, Staged& sg) {
   if (n < 0 || (n > 0 && (!pts || !nrm || !rad)))
