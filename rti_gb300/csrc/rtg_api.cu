@@ -915,7 +915,7 @@ static int rtg_autotune_body(rtg_context* ctx, uint64_t sample_rays, uint64_t se
               if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
               if (stack == 256 && stack_for(0, traversal_depth(ctx)) == 256) continue;
               if (leaf == RTG_LEAF_POSTPONED && packet == 32) continue;
-              cand.push_back(Cand{builder, width, rtg_launch_config{tpb, packet, stack, sched, leaf}, 0.0f});
+              cand.push_back(Cand{builder, width, rtg_launch_config{tpb, packet, stack, sched, leaf, RTG_STACK_AUTO}, 0.0f});
             }
     float ms = 0.0f;
     for (size_t i = first; i < cand.size() && rc == RTG_OK; ++i) {

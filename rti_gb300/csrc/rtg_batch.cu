@@ -444,7 +444,7 @@ static int rtg_batch_autotune_body(rtg_batch* b, double fraction, rtg_launch_con
             if (sched == RTG_SCHED_PLAIN && (packet != 1 || tpb == 64 || stack != 0)) continue;
             if (stack == 256 && stack_for(0, b->depth) == 256) continue;
             if (leaf == RTG_LEAF_POSTPONED && packet == 32) continue;
-            cand.push_back(rtg_launch_config{tpb, packet, stack, sched, leaf});
+            cand.push_back(rtg_launch_config{tpb, packet, stack, sched, leaf, RTG_STACK_AUTO});
           }
   std::vector<float> tms(cand.size(), 0.0f);
   float ms = 0.0f;

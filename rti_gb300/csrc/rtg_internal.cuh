@@ -223,7 +223,7 @@ struct rtg_context {
   bool traced = false;
   bool finalized = false;
   float box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
-  rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL, RTG_LEAF_IMMEDIATE};
+  rtg_launch_config lc{128, 1, 0, RTG_SCHED_MEGAKERNEL, RTG_LEAF_IMMEDIATE, RTG_STACK_AUTO};
   int32_t node_width = 0;  // RTG_NODES_*: closest hits over the binary or the wide tree
   int32_t deposit_mode = RTG_DEPOSIT_NEIGHBORS;
   int32_t accum = RTG_ACCUM_FP64;
