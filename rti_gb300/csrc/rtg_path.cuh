@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
   const unsigned lt_mask = (1u << lane) - 1u;
   // per-lane counters, summed over the warp at the end (32 bits: a lane traces
   // far fewer than 2^32 segments)
-  uint32_t c_hit = 0, c_non = 0, c_tot = 0, c_seg = 0, c_trunc = 0, c_nb = 0, c_err = 0;
+  uint32_t c_hit = 0, c_non = 0, c_tot = 0, c_seg = 0, c_nb = 0, c_err = 0;
   bool active = false, exhausted = false;
   uint64_t id = 0;
   f3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
@@ -736,7 +736,7 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
     if (!active) continue;
     // ---- one segment (tracer.hpp:169-279) ----
     if (nseg == pp->max_segments) {
-      c_trunc += 1;
+      atomicAdd(&p0.tally->truncated, 1ull);  // rare: no per-lane counter
       active = path_end();
       continue;
     }
@@ -774,7 +774,7 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
       } else {
         if (kAdj) G = __ldg(&pp->adj_g[hid]);
         else deposit(*pp, hid, v);
-        c_tot += 1;
+        if (M == kModeWindow) c_tot += 1;  // elsewhere total = hits + neighbour deposits
       }
       if (M != kModeWindow && !(href & kTriBit) && pp->s.nb_ptr) {  // tracer.hpp:339-383
         const int64_t q0 = __ldg(&pp->s.nb_ptr[hid]), q1 = __ldg(&pp->s.nb_ptr[hid + 1]);
@@ -796,7 +796,6 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
           if (local_intersect(o, d, mk3(cr.x, cr.y, cr.z), cr.w, mk3(nv.x, nv.y, nv.z))) {
             if (kAdj) G += __ldg(&pp->adj_g[nb]);
             else deposit(*pp, nb, v);
-            c_tot += 1;
             c_nb += 1;
           }
         }
@@ -896,15 +895,15 @@ __global__ void __launch_bounds__(TPB, (M == kModeForward && TPB == 128 ? 1152 :
       atomicAdd(&pp->adj_scalars[1], acc_n);
     }
   }
-  const unsigned long long s_hit = warp_sum(c_hit), s_non = warp_sum(c_non), s_tot = warp_sum(c_tot);
-  const unsigned long long s_seg = warp_sum(c_seg), s_trunc = warp_sum(c_trunc), s_nb = warp_sum(c_nb);
+  const unsigned long long s_hit = warp_sum(c_hit), s_non = warp_sum(c_non);
+  const unsigned long long s_seg = warp_sum(c_seg), s_nb = warp_sum(c_nb);
+  const unsigned long long s_tot = M == kModeWindow ? warp_sum(c_tot) : s_hit + s_nb;
   const unsigned long long s_err = warp_sum(c_err);
   if (lane == 0) {
     atomicAdd(&p0.tally->hitc, s_hit);
     atomicAdd(&p0.tally->nonhitc, s_non);
     atomicAdd(&p0.tally->total, s_tot);
     atomicAdd(&p0.tally->segments, s_seg);
-    atomicAdd(&p0.tally->truncated, s_trunc);
     atomicAdd(&p0.tally->nb_deposits, s_nb);
     atomicAdd(&p0.tally->errors, s_err);
   }
