@@ -226,6 +226,36 @@ def test_reader_errors(tmp_path):
         vtk.read_point_cloud(str(f))
 
 
+def test_reader_rejects_damaged_data(tmp_path):
+    """Sizes and offsets read from a file are checked against the file before
+    anything is read or allocated: a damaged header is an error, not a read
+    past the data or a huge allocation."""
+    p, n, r = _discs(5)
+    arrays = [("CellData", "nn", n.astype(np.float64).ravel(), 3), ("CellData", "radius", r.astype(np.float64), 1),
+              ("Points", "Points", p.astype(np.float64).ravel(), 3)]
+    good = tmp_path / "good.vtp"
+    _write_encoded(good, arrays, "raw", "UInt64")
+    vtk.read_point_cloud(str(good))  # the undamaged file reads
+    data = good.read_bytes()
+    at = data.index(b'encoding="raw">\n_') + len(b'encoding="raw">\n_')
+    cases = {
+        "huge array size": data[:at] + (1 << 60).to_bytes(8, "little") + data[at + 8:],
+        "array size that wraps": data[:at] + ((1 << 64) - 1).to_bytes(8, "little") + data[at + 8:],
+        "offset past the end": data.replace(b'offset="0"', b'offset="99999999"', 1),
+    }
+    _write_encoded(good, arrays, "base64", "UInt64")
+    cases["base64 offset past the end"] = good.read_bytes().replace(b'offset="0"', b'offset="99999999"', 1)
+    _write_encoded(good, arrays, "raw", "UInt64", compress=True)
+    z = good.read_bytes()
+    zat = z.index(b'encoding="raw">\n_') + len(b'encoding="raw">\n_')
+    cases["huge block count"] = z[:zat] + (1 << 61).to_bytes(8, "little") + z[zat + 8:]
+    for name, blob in cases.items():
+        f = tmp_path / "bad.vtp"
+        f.write_bytes(blob)
+        with pytest.raises(RtgError, match="out of range|truncated|compressed"):
+            vtk.read_point_cloud(str(f))
+
+
 def test_segment_log_vtp_writer(rtg_lib, tmp_path):
     """rtg_write_vtp_segments (no GPU): one line cell per segment, two points
     each (origin, end), the cell arrays in record order."""
