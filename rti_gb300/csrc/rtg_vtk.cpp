@@ -391,8 +391,14 @@ bool host_little() {
 }
 
 // Reads header word k of a binary block header.
+// Header word k (hs = 4 or 8 bytes), read as an integer straight from the
+// bytes (through a double, sizes above 2^53 would round and some wrap).
 uint64_t header_word(const std::vector<unsigned char>& h, size_t k, size_t hs, bool swap) {
-  return (uint64_t)load_value(h.data() + k * hs, hs == 8 ? "UInt64" : "UInt32", swap);
+  const unsigned char* p = h.data() + k * hs;
+  const bool big = host_little() ? swap : !swap;  // the file's byte order
+  uint64_t v = 0;
+  for (size_t i = 0; i < hs; ++i) v |= (uint64_t)p[big ? hs - 1 - i : i] << (8 * i);
+  return v;
 }
 
 bool inflate_blocks(const std::vector<unsigned char>& header, const unsigned char* data, size_t avail, size_t hs,
