@@ -299,7 +299,10 @@ RTG_API int rtg_synchronize(rtg_context* ctx);
 /* Asks a running trace to stop; it returns RTG_ERR_ABORTED. */
 RTG_API int rtg_request_abort(rtg_context* ctx);
 
-/* Per-primitive sticking from a device array (e.g. a torch tensor); NULL clears it. */
+/* Per-primitive sticking from a device array (e.g. a torch tensor), copied
+ * into the context on `stream` (the caller's array may be freed or reused
+ * after that copy in stream order); NULL clears it.  The values are not
+ * checked: each must lie in [0, 1]. */
 RTG_API int rtg_set_sticking_field_device(rtg_context* ctx, const float* d_field, int64_t n, void* stream);
 
 /* Adjoint of the trace (no counterpart in rti; the differentiation path).
