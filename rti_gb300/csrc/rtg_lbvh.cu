@@ -337,6 +337,152 @@ __global__ void ploc_merge_kernel(const uint32_t* __restrict__ nn, int64_t bound
   }
 }
 
+// The last rounds of PLOC in one block: once at most kPlocTailMax clusters
+// remain, the rounds are too small to fill the GPU and a launch sequence per
+// round (neighbours, flags, scan, merge) costs more than the work.  One block
+// of kPlocTailThreads runs every remaining round with the same rules as the
+// kernels above -- nearest neighbour within kPlocRadius positions (ties to the
+// lower position), mutual pairs merged by the lower member, survivors
+// compacted in order, nodes handed out downwards in position order -- so the
+// tree is the one the round-by-round launches would build.  Each round merges
+// at least the pair of smallest merged area, so the loop ends after at most
+// n - 1 rounds (n_int + 1 bounds it); a round without a merge sets state[2]
+// and stops.
+constexpr uint32_t kPlocTailMax = 8192;  // measured: 2 Ki-8 Ki fastest on the hole (200 k leaves)
+constexpr int kPlocTailThreads = 1024;
+
+__global__ void __launch_bounds__(kPlocTailThreads) ploc_tail_kernel(
+    uint32_t* __restrict__ cid0, float4* __restrict__ blo0, float4* __restrict__ bhi0, uint32_t* __restrict__ cid1,
+    float4* __restrict__ blo1, float4* __restrict__ bhi1, uint32_t* __restrict__ nn, uint64_t* __restrict__ state,
+    uint32_t n_int, const uint32_t* __restrict__ leaf_ref, int64_t nleaves, Node* __restrict__ nodes,
+    uint32_t* __restrict__ parent) {
+  __shared__ uint32_t w_keep[kPlocTailThreads / 32], w_merge[kPlocTailThreads / 32];
+  __shared__ uint32_t s_tot[2];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  uint32_t n = (uint32_t)state[0];
+  uint32_t allocated = (uint32_t)state[1];
+  uint32_t* cid_in = cid0;
+  float4* blo_in = blo0;
+  float4* bhi_in = bhi0;
+  uint32_t* cid_out = cid1;
+  float4* blo_out = blo1;
+  float4* bhi_out = bhi1;
+  bool stalled = false;
+  for (uint32_t round = 0; n > 1 && round < n_int + 1u; ++round) {
+    for (uint32_t i = tid; i < n; i += kPlocTailThreads) {
+      const float4 al = blo_in[i], ah = bhi_in[i];
+      float best = INFINITY;
+      uint32_t bj = i > 0 ? i - 1 : i + 1;
+      for (int d = -kPlocRadius; d <= kPlocRadius; ++d) {
+        const int64_t j = (int64_t)i + d;
+        if (d == 0 || j < 0 || j >= (int64_t)n) continue;
+        const float a = merged_area(al, ah, blo_in[j], bhi_in[j]);
+        if (a < best) {
+          best = a;
+          bj = (uint32_t)j;
+        }
+      }
+      nn[i] = bj;
+    }
+    __syncthreads();
+    // survivors and merges of this thread's run of positions, then their
+    // exclusive prefix over the block (positions in order)
+    const uint32_t per = (n + kPlocTailThreads - 1) / kPlocTailThreads;
+    const uint32_t c0 = min(n, tid * per), c1 = min(n, c0 + per);
+    uint32_t keep = 0, merge = 0;
+    for (uint32_t i = c0; i < c1; ++i) {
+      const uint32_t j = nn[i];
+      const bool mutual = nn[j] == i;
+      keep += (mutual && i > j) ? 0u : 1u;
+      merge += (mutual && i < j) ? 1u : 0u;
+    }
+    uint32_t ik = keep, im = merge;  // inclusive warp scan
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t k2 = __shfl_up_sync(0xFFFFFFFFu, ik, o), m2 = __shfl_up_sync(0xFFFFFFFFu, im, o);
+      if (lane >= (uint32_t)o) {
+        ik += k2;
+        im += m2;
+      }
+    }
+    if (lane == 31) {
+      w_keep[warp] = ik;
+      w_merge[warp] = im;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t tk = lane < kPlocTailThreads / 32 ? w_keep[lane] : 0u, tm = lane < kPlocTailThreads / 32 ? w_merge[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t k2 = __shfl_up_sync(0xFFFFFFFFu, tk, o), m2 = __shfl_up_sync(0xFFFFFFFFu, tm, o);
+        if (lane >= (uint32_t)o) {
+          tk += k2;
+          tm += m2;
+        }
+      }
+      if (lane < kPlocTailThreads / 32) {  // inclusive prefix over the warps
+        w_keep[lane] = tk;
+        w_merge[lane] = tm;
+      }
+      if (lane == kPlocTailThreads / 32 - 1) {
+        s_tot[0] = tk;
+        s_tot[1] = tm;
+      }
+    }
+    __syncthreads();
+    uint32_t pos = (warp > 0 ? w_keep[warp - 1] : 0u) + ik - keep;
+    uint32_t rank = (warp > 0 ? w_merge[warp - 1] : 0u) + im - merge;
+    const uint32_t kept_total = s_tot[0], merged_total = s_tot[1];
+    const uint32_t node_top = n_int - 1u - allocated;
+    for (uint32_t i = c0; i < c1; ++i) {
+      const uint32_t j = nn[i];
+      const bool mutual = nn[j] == i;
+      if (mutual && i > j) continue;  // absorbed by j
+      if (mutual) {
+        const uint32_t idx = node_top - rank++;
+        const uint32_t a = cid_in[i], b = cid_in[j];
+        const uint32_t ra = (a & kClusterLeaf) ? leaf_ref[a & ~kClusterLeaf] : a;
+        const uint32_t rb = (b & kClusterLeaf) ? leaf_ref[b & ~kClusterLeaf] : b;
+        nodes[idx].d = make_uint4(ra, rb, 0u, 0u);
+        if (a & kClusterLeaf) parent[(nleaves - 1) + (a & ~kClusterLeaf)] = idx;
+        else parent[a] = idx;
+        if (b & kClusterLeaf) parent[(nleaves - 1) + (b & ~kClusterLeaf)] = idx;
+        else parent[b] = idx;
+        const float4 al = blo_in[i], ah = bhi_in[i], bl = blo_in[j], bh = bhi_in[j];
+        cid_out[pos] = idx;
+        blo_out[pos] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.0f);
+        bhi_out[pos] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f);
+      } else {
+        cid_out[pos] = cid_in[i];
+        blo_out[pos] = blo_in[i];
+        bhi_out[pos] = bhi_in[i];
+      }
+      ++pos;
+    }
+    __syncthreads();  // the outputs are complete before they become the inputs
+    if (merged_total == 0) {
+      stalled = true;
+      break;
+    }
+    allocated += merged_total;
+    n = kept_total;
+    uint32_t* tc = cid_in;
+    cid_in = cid_out;
+    cid_out = tc;
+    float4* tl = blo_in;
+    blo_in = blo_out;
+    blo_out = tl;
+    float4* th = bhi_in;
+    bhi_in = bhi_out;
+    bhi_out = th;
+  }
+  if (tid == 0) {
+    state[0] = n;
+    state[1] = allocated;
+    if (stalled || n > 1) state[2] = 1;
+  }
+}
+
 __device__ __forceinline__ void child_box(uint32_t ref, const float4* __restrict__ dn,
                                           const float4* __restrict__ tri, const float* __restrict__ plo,
                                           const float* __restrict__ phi, const float* node_box, float* lo,
@@ -564,7 +710,12 @@ int build_ploc(rtg_context* ctx, const uint32_t* d_sorted_prim, cudaStream_t st)
       rc = set_error(ctx, RTG_ERR_INTERNAL, "PLOC did not converge");
       break;
     }
-    for (int r = 0; r < 4 && rc == RTG_OK; ++r) {
+    if (h[0] <= kPlocTailMax) {  // the remaining rounds in one block
+      ploc_tail_kernel<<<1, kPlocTailThreads, 0, st>>>(cid[q].p, blo[q].p, bhi[q].p, cid[q ^ 1].p, blo[q ^ 1].p,
+                                                        bhi[q ^ 1].p, nn.p, state.p, n_int, g.leaf_ref.p, n,
+                                                        g.nodes.p, g.parent.p);
+    }
+    for (int r = 0; r < 4 && rc == RTG_OK && h[0] > kPlocTailMax; ++r) {
       const unsigned nb = (unsigned)((bound + kPlocThreads - 1) / kPlocThreads);
       ploc_nn_kernel<<<nb, kPlocThreads, 0, st>>>(blo[q].p, bhi[q].p, state.p, nn.p);
       ploc_flags_kernel<<<blocks_for(bound, 256), 256, 0, st>>>(nn.p, bound, state.p,
