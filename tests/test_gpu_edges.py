@@ -130,3 +130,27 @@ def test_refused_upload_keeps_the_surface(eng):
     assert eng.num_primitives == t.n
     eng.trace(50000, 3)
     assert np.array_equal(eng.hit_counts(), before)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 8192, 8193, 20000])
+def test_ploc_sizes_around_the_single_block_tail(eng, oracle_lib, n):
+    """PLOC builds whose last rounds run in one block (at most 8 Ki clusters)
+    and builds that reach it after round-by-round launches: each builds
+    without error and traces as the oracle does."""
+    from rti_gb300 import _lib as L
+    rng = np.random.default_rng(n)
+    c = np.stack([rng.uniform(0, 1, n), rng.uniform(0, 1, n), rng.uniform(-0.5, 0, n)], 1).astype(np.float32)
+    nrm = rng.normal(size=(n, 3)) + [0, 0, 1.5]
+    nrm = (nrm / np.linalg.norm(nrm, axis=1)[:, None]).astype(np.float32)
+    r = rng.uniform(0.003, 0.02, n).astype(np.float32)
+    eng.set_tree_builder(L.RTG_TREE_PLOC)
+    try:
+        eng.upload_discs(c, nrm, r)
+        assert 1 <= eng.tree_depth <= 256 or n == 1
+        s = oracle_lib.Scene(np.concatenate([c, r[:, None]], 1), nrm)
+        s.neighbors(bruteforce=True)
+        lo, hi = np.array([0, 0, -0.6], np.float32), np.array([1, 1, 0.1], np.float32)
+        _compare(eng, oracle_lib, s, dict(box_lo=lo, box_hi=hi, sticking=0.3), n=5000, box=_box(lo, hi),
+                 x_bound=1, y_bound=1, sticking=0.3)
+    finally:
+        eng.set_tree_builder(L.RTG_TREE_KARRAS)
