@@ -630,6 +630,8 @@ def run_case(args):
     traces, then --steps traces of --rays rays; one JSON line."""
     from rti_gb300 import Engine, scenes
     from rti_gb300 import _lib as L
+    if args.case == "batch":
+        return run_batch_case(args)
     with Engine(0) as e:
         e.set_node_width(args.node_width)
         if args.case == "hole":
@@ -658,6 +660,43 @@ def run_case(args):
         print(json.dumps({"case": args.case, "rays": args.rays, "node_width": args.node_width,
                           "kernel_ms": [round(t_.kernel_ms, 3) for t_ in rows], "segments": rows[-1].segments,
                           "hitc": rows[-1].hitc, "nb_deposits": rows[-1].nb_deposits, "errors": rows[-1].errors}))
+
+
+def run_batch_case(args):
+    """The batch block's 192 jobs (64 surfaces x 3 species, --batch-rays rays
+    each) in one graph-replayed launch with the launch shape the autotuner
+    picks for them (64 threads, 256-entry stack): two warm-up runs, then
+    --steps timed runs; one JSON line.  The target of the batch's ncu captures."""
+    from rti_gb300 import Engine, scenes
+    from rti_gb300.batch import Batch
+    inst = scenes.batch_instances(n=64, seed=0)
+    engines, b = [], Batch(0)
+    try:
+        for s in inst:
+            e = Engine(0)
+            engines.append(e)
+            e.set_node_width(args.node_width)
+            e.upload_discs(s.points, s.normals, s.radii)
+            e.configure(box=(s.box_lo, s.box_hi), x_bound=1, y_bound=1, reset=True)
+            for stick, expo in scenes.BATCH_SPECIES:
+                c = e.config()
+                c.sticking, c.source_exponent = stick, expo
+                b.add(e, args.batch_rays, seed=0, config=c)
+        b.set_launch_config(threads_per_block=64, stack_depth=256)
+        ms = []
+        for k in range(2 + args.steps):
+            b.run(use_graph=True)
+            t = b.synchronize()
+            if k >= 2:
+                ms.append(t)
+        tb = b.tally()
+        print(json.dumps({"case": "batch", "jobs": len(b), "rays": len(b) * args.batch_rays,
+                          "batched_ms": [round(x, 3) for x in ms], "segments": tb.segments, "hitc": tb.hitc,
+                          "errors": tb.errors}))
+    finally:
+        b.close()
+        for e in engines:
+            e.close()
 
 
 def ray_sweep(eng, sizes):
@@ -706,7 +745,7 @@ def main():
                                                 "(the tail analysis), printed instead of the bench line")
     ap.add_argument("--rough-rays", type=int, default=100_000_000, help="rays of the rough-surface block")
     ap.add_argument("--rough-only", action="store_true", help="run the rough-surface block alone and print it")
-    ap.add_argument("--case", default="", choices=["", "hole", "trench", "rough"],
+    ap.add_argument("--case", default="", choices=["", "hole", "trench", "rough", "batch"],
                     help="time the path kernel on one workload alone (--rays, --steps, --node-width)")
     ap.add_argument("--node-width", type=int, default=0, choices=[0, 2, 8],
                     help="tree of the closest-hit queries: 0 automatic, 2 binary, 8 compressed 8-wide")
