@@ -729,7 +729,7 @@ def main():
     ap.add_argument("--cpu-rays", type=int, default=2_000_000, help="CPU-baseline sample (ours arm)")
     ap.add_argument("--ref-rays", type=int, default=2_000_000,
                     help="source rays timed per step of the reference arm (a sample of the step's rays)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
