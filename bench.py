@@ -502,7 +502,8 @@ def run_ours(args):
                "d2h_bytes_per_step": int(16 * np_),
                "includes": "per step: upload of the surface from pinned host arrays (checks, LBVH build), "
                            "configuration, trace, hit counts + S1 read back into pinned host arrays, on a "
-                           "context kept across steps",
+                           "context kept across steps" + ("; per rank, without the cross-rank sum" if world > 1
+                                                          else ""),
                "fresh_context_value": world * R / statistics.mean(fresh_times),
                "fresh_context_includes": "the same with a context created and destroyed every step"}
 
