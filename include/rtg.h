@@ -349,7 +349,9 @@ RTG_API int rtg_get_tally(rtg_context* ctx, rtg_tally* out);
  * on (seed, ray id), so the result equals the trace of [0, n) in one go: the
  * same hit counts and tallies, S1 bit for bit under RTG_ACCUM_FIXED (S2..S4
  * and plain S1 up to the order of the FP64 additions).  All five arrays hold
- * rtg_num_primitives values; the tally's timings are ignored. */
+ * rtg_num_primitives values; the tally's timings are ignored.  The call waits
+ * for the device to finish its work (a trace of this context may still be
+ * writing the accumulators) before it replaces them. */
 RTG_API int rtg_set_accumulators(rtg_context* ctx, const double* s1, const double* s2, const double* s3,
                                  const double* s4, const uint64_t* counts, const rtg_tally* tally);
 /* Neighbour CSR of the discs: row_ptr (nd+1), cols (cap entries); *nnz gets the count. */
