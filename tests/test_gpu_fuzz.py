@@ -193,3 +193,39 @@ def test_random_batch(rtg_lib, oracle_lib):
         ref = s.trace(cfg, 0, N_RAYS + 100 * i, sticking_field=c["field"])
         assert np.array_equal(cnt, ref.counts), i
         np.testing.assert_allclose(s1, ref.s1, rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("k", range(0, CASES, 2))
+def test_random_explicit_rays(eng, oracle_lib, k):
+    """rtg_trace_rays on the random surfaces over both trees: 20,000 random
+    rays (origins in and around the surface, directions uniform on the sphere,
+    some axis-parallel) give the same primitive ids and distances, bit for bit,
+    as the oracle's closest hit."""
+    c = _case(k)
+    lo, hi = c["box"]
+    rng = np.random.default_rng(11000 + k)
+    n = 20000
+    o = rng.uniform(lo - 0.2, hi + 0.2, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    ax = rng.random(n) < 0.05  # axis-parallel directions
+    d[ax] = np.eye(3)[rng.integers(0, 3, ax.sum())] * rng.choice([-1.0, 1.0], size=(ax.sum(), 1))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    if c["kind"] == "discs":
+        eng.upload_discs(c["points"], c["normals"], c["radii"])
+    elif c["kind"] == "triangles":
+        eng.upload_triangles(c["vertices"], c["indices"])
+    else:
+        eng.upload_mixed(c["points"], c["normals"], c["radii"], c["vertices"], c["indices"])
+    xyzr = (np.concatenate([c["points"], c["radii"][:, None]], 1) if "points" in c else None)
+    s = oracle_lib.Scene(xyzr, c.get("normals"), c.get("vertices"), c.get("indices"))
+    pc, tc = s.closest_hit(rays)
+    for width in (2, 8):
+        eng.set_node_width(width)
+        try:
+            pg, tg = eng.trace_rays(rays)
+        finally:
+            eng.set_node_width(0)
+        assert np.array_equal(pg, pc), width
+        assert np.array_equal(tg.view(np.uint32), tc.view(np.uint32)), width
+    assert (pc >= 0).any()
