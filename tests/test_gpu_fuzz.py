@@ -229,3 +229,49 @@ def test_random_explicit_rays(eng, oracle_lib, k):
         assert np.array_equal(pg, pc), width
         assert np.array_equal(tg.view(np.uint32), tc.view(np.uint32)), width
     assert (pc >= 0).any()
+
+
+def _log_cases():
+    out = []
+    for k in range(CASES):
+        c = _case(k)
+        if c["field"] is None and not c["window"]:
+            out.append(k)
+    return out[:10]
+
+
+@pytest.mark.parametrize("k", _log_cases())
+def test_random_segment_logs(eng, oracle_lib, k):
+    """Every segment of the first 400 paths on random surfaces (origin, end
+    point, kind, primitive, weight), GPU segment log against the oracle's
+    per-path log, bit for bit."""
+    c = _case(k)
+    lo, hi = c["box"]
+    n = 400
+    eng.set_node_width(c["width"])
+    if c["kind"] == "discs":
+        eng.upload_discs(c["points"], c["normals"], c["radii"])
+    elif c["kind"] == "triangles":
+        eng.upload_triangles(c["vertices"], c["indices"])
+    else:
+        eng.upload_mixed(c["points"], c["normals"], c["radii"], c["vertices"], c["indices"])
+    eng.configure(box=(lo, hi), reset=True, **c["cfg"])
+    eng.set_segment_log(0, n, 1 << 22)
+    try:
+        eng.trace(n, seed=c["seed"])
+        log, dropped = eng.segment_log()
+    finally:
+        eng.set_segment_log(0, 0, 0)
+        eng.set_node_width(0)
+    assert dropped == 0
+    xyzr = (np.concatenate([c["points"], c["radii"][:, None]], 1) if "points" in c else None)
+    s = oracle_lib.Scene(xyzr, c.get("normals"), c.get("vertices"), c.get("indices"))
+    if s.nd:
+        s.neighbors(bruteforce=True)
+    cfg = oracle_lib.make_config(lo, hi, seed=c["seed"], **c["cfg"])
+    ref = np.concatenate([oracle_lib.trace_log(s, cfg, i) for i in range(n)])
+    assert len(log) == len(ref)
+    for f in ("ray", "segment", "kind", "primitive"):
+        assert np.array_equal(log[f], ref[f]), f
+    for f in ("org", "end", "weight"):
+        assert np.array_equal(log[f].view(np.uint32), ref[f].view(np.uint32)), f
